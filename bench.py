@@ -1,0 +1,356 @@
+"""GEMM-family throughput on GB300: split-BF16 tcgen05 vs plain FP32 SIMT.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one C = alpha*A*B + beta*C over N x N FP32 matrices (polybench gemm
+initialisation, alpha=32412, beta=2123, N=8192 by default), all operands
+resident in HBM.  Prints one JSON line (rank 0).  Under torchrun every rank
+runs an independent replica on its own GPU (the contraction has no exchange
+step), so scaling is weak and `value` sums all ranks' work over the slowest
+rank's time.
+
+`--impl reference` times the reference's CPU implementation of the same
+kernel body (gemm.cpp:82-91) on the host cores, through the oracle's port of
+it, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "sycl-bench_gb300"))
+
+import numpy as np  # noqa: E402
+
+ALPHA, BETA = 32412.0, 2123.0
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+# ------------------------------------------------------------------ helpers
+def polybench_gemm_init(n: int):
+    """gemm.cpp:18-40 in float32 arithmetic: A=i*k/N, B=(k*j+1)/N, C=(i*j+2)/N."""
+    i = np.arange(n, dtype=np.float32)[:, None]
+    j = np.arange(n, dtype=np.float32)[None, :]
+    nf = np.float32(n)
+    ij = i * j
+    return ij / nf, (ij + np.float32(1)) / nf, (ij + np.float32(2)) / nf
+
+
+def load_peaks() -> tuple[dict, str]:
+    if PEAKS_FILE.exists():
+        try:
+            return json.loads(PEAKS_FILE.read_text()), "measured"
+        except (OSError, ValueError):
+            pass
+    return dict(FALLBACK_PEAKS), "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms in a thread."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples: list[tuple[float, list[str]]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self) -> None:
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self) -> None:
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self) -> None:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float) -> dict:
+        window = "timed"
+        rows = [s for t, s in self.samples if t0 <= t <= t1]
+        if len(rows) < 3:  # timed region shorter than a few sampling periods: widen to the loaded phase
+            rows = [s for _, s in self.samples if len(s) > 4 and s[4].isdigit() and int(s[4]) > 0]
+            window = "loaded phase (timed region shorter than the sampling period)"
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(r[1]) for r in rows) if v is not None]
+        smax = [v for v in (num(r[2]) for r in rows) if v is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if len(r) > 6 + k and r[6 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows), "window": window,
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+class Dist:
+    """torchrun rendezvous for replicas: barrier and max-over-ranks only."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            td.init_process_group(backend=backend)
+            self.td, self.torch, self.backend = td, torch, backend
+
+    def barrier(self) -> None:
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        dev = f"cuda:{self.local_rank}" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ------------------------------------------------------------ GPU workload
+def run_gpu(args, dist: Dist) -> dict | None:
+    import gbpoly
+    from gbpoly import Precision
+
+    n = args.size
+    nbytes = n * n * 4
+    flops = 2.0 * n ** 3
+    ctx = gbpoly.Context(dist.local_rank)
+    props = ctx.device_props()
+    A, B, C = polybench_gemm_init(n)
+    dA, dB, dC, dC0 = ctx.upload(A), ctx.upload(B), ctx.upload(C), ctx.upload(C)
+
+    # FP64 oracle on the GPU (DGEMM) for the error of each form
+    dA64, dB64, dR = ctx.alloc(2 * nbytes), ctx.alloc(2 * nbytes), ctx.alloc(2 * nbytes)
+    ctx.convert_f32_f64(dA, dA64, n * n)
+    ctx.convert_f32_f64(dB, dB64, n * n)
+    ctx.convert_f32_f64(dC0, dR, n * n)
+    ctx.gemm_f64(n, n, n, ALPHA, dA64, n, dB64, n, BETA, dR, n)
+    ctx.synchronize()
+    ctx.free(dA64)
+    ctx.free(dB64)
+
+    def one(prec):
+        ctx.gemm(prec, n, n, n, ALPHA, dA, n, dB, n, BETA, dC, n)
+
+    def fresh_c():
+        ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(dC), gbpoly._ptr(dC0), nbytes)
+
+    forms = [Precision.FP32]
+    headline = Precision.FP32
+    tiers = {}
+    sampler = ClockSampler(dist.local_rank)
+    sampler.start()
+    timed_window = (0.0, 0.0)
+    for prec in forms:
+        fresh_c()
+        one(prec)
+        ctx.synchronize()
+        max_rel, frob, elem = ctx.error_norms(dC, n, dR, n, n, n)
+        for _ in range(args.warmup):
+            one(prec)
+        ctx.synchronize()
+        ev0, ev1 = ctx.event(), ctx.event()
+        dist.barrier()
+        ctx.synchronize()
+        t0 = time.time()
+        ev0.record()
+        for _ in range(args.steps):
+            one(prec)
+        ev1.record()
+        ctx.synchronize()
+        t1 = time.time()
+        dist.barrier()
+        ms = ev0.elapsed_ms(ev1) / args.steps
+        ms = dist.max(ms)
+        if prec == headline:
+            timed_window = (t0, t1)
+        tiers[prec.name.lower()] = {
+            "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12 * dist.world,
+            "err_vs_fp64": {"max_rel": max_rel, "frob_rel": frob, "max_elem_rel": elem},
+            "kernel_launches_per_step": 1,
+        }
+        ev0.destroy()
+        ev1.destroy()
+    sampler.stop()
+    clocks = sampler.summary(*timed_window)
+
+    # ---- end to end through the C ABI: pinned host buffers, copies inside the timed region
+    import ctypes as ct
+    hbuf = []
+    for arr in (A, B, C):
+        p = ct.c_void_p()
+        gbpoly._check(ctx.lib.gbpoly_host_alloc(ctx.handle, ct.byref(p), nbytes))
+        ct.memmove(p.value, arr.ctypes.data, nbytes)
+        hbuf.append(p.value)
+    pout = ct.c_void_p()
+    gbpoly._check(ctx.lib.gbpoly_host_alloc(ctx.handle, ct.byref(pout), nbytes))
+    hA, hB, hC, hOut = hbuf[0], hbuf[1], hbuf[2], pout.value
+
+    def e2e_step():
+        for dst, src in ((dA, hA), (dB, hB), (dC, hC)):
+            gbpoly._check(ctx.lib.gbpoly_memcpy_h2d(ctx.handle, gbpoly._ptr(dst), ct.c_void_p(src), nbytes))
+        one(headline)
+        gbpoly._check(ctx.lib.gbpoly_memcpy_d2h(ctx.handle, ct.c_void_p(hOut), gbpoly._ptr(dC), nbytes))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    ctx.synchronize()
+    dist.barrier()
+    e0, e1 = ctx.event(), ctx.event()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    ctx.synchronize()
+    e2e_ms = dist.max(e0.elapsed_ms(e1) / args.steps)
+    for p in (hA, hB, hC, hOut):
+        ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
+
+    head = tiers[headline.name.lower()]
+    peaks, peak_kind = load_peaks()
+    if headline == Precision.FP32:
+        # FFMA pipe: SMs x 128 lanes x 2 FLOP x max SM clock (no measured FP32 figure exists)
+        clk_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or props["sm_clock_khz"] / 1e3
+        peak = props["sm_count"] * 128 * 2 * clk_mhz * 1e6 / 1e12
+        roof = {"bound": "fp32_simt", "achieved": head["tflops"] / dist.world, "peak": peak, "unit": "TFLOP/s",
+                "frac": head["tflops"] / dist.world / peak, "traffic": None,
+                "peak_source": f"computed: {props['sm_count']} SMs x 128 FFMA lanes x 2 x {clk_mhz:.0f} MHz"}
+    ctx.close()
+    return {
+        "value": head["tflops"], "ms_per_step": head["ms_per_step"], "tiers": tiers, "clocks": clocks,
+        "roofline": roof, "headline": headline.name.lower(),
+        "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 * dist.world, "unit": "TFLOP/s",
+                "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps * head["kernel_launches_per_step"],
+        "device": props, "peak_kind": peak_kind,
+    }
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_gemm_sample(n: int, target_s: float) -> dict:
+    """The reference kernel body (gemm.cpp:82-91) on the host cores through the
+    oracle's port, on the first `rows` output rows, `rows` grown until one sample
+    takes about `target_s` seconds."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    lib = oracle.fast_lib()
+    A, B, C = polybench_gemm_init(n)
+    rows = 1
+    while True:
+        t = time.perf_counter()
+        lib.orc_gemm_body(A, B, C, n, 0, rows, ALPHA, BETA)
+        dt = time.perf_counter() - t
+        if dt >= target_s or rows >= n:
+            break
+        rows = min(n, max(rows * 2, int(rows * target_s / max(dt, 1e-3) * 0.9)))
+    return {"rows": rows, "seconds": dt, "tflops": 2.0 * rows * n * n / dt / 1e12,
+            "cores": lib.orc_num_threads()}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--size", type=int, default=8192)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist = Dist()
+    n = args.size
+    config = {"workload": f"polybench gemm C=alpha*A*B+beta*C, N={n} (NI=NJ=NK), alpha=32412, beta=2123, "
+                          f"polybench init A=i*k/N B=(k*j+1)/N C=(i*j+2)/N",
+              "size": n, "flops_per_step": 2 * n ** 3, "l2": "inputs larger than L2 (3 x N^2 x 4 B), no flush",
+              "parallelism": f"replicas x{dist.world}"}
+    base = {"metric": "GEMM-family TFLOP/s (split-BF16 tcgen05 vs plain FP32 SIMT, matched FP64 error)",
+            "unit": "TFLOP/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic (analytic polybench init)",
+            "config": config}
+
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        samples = []
+        for s in range(args.warmup + args.steps):
+            r = cpu_gemm_sample(n, min(args.cpu_seconds, 8.0))
+            if s >= args.warmup:
+                samples.append(r)
+        best = max(samples, key=lambda r: r["tflops"])
+        val = statistics.median(r["tflops"] for r in samples)
+        line = dict(base, impl="reference", value=val, ms_per_step=statistics.median(
+            r["seconds"] * 1e3 for r in samples), dtype="f32",
+            cpu_baseline={"value": val, "unit": "TFLOP/s", "cores": best["cores"], "kind": "port",
+                          "sample": f"first {best['rows']} of {n} output rows of the gemm.cpp:82-91 kernel body, "
+                                    f"OpenMP over (row, 64-wide column block), -O3 -march=native -ffast-math"},
+            e2e={"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+        print(json.dumps(line))
+        dist.close()
+        return
+
+    res = run_gpu(args, dist)
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        r = cpu_gemm_sample(n, args.cpu_seconds)
+        cpu = {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["cores"], "kind": "port",
+               "sample": f"first {r['rows']} of {n} output rows of the gemm.cpp:82-91 kernel body on the host "
+                         f"cores ({r['seconds']:.1f} s), oracle port built -O3 -march=native -ffast-math"}
+    if dist.rank == 0:
+        line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"],
+                    dtype="f32" if res["headline"] == "fp32" else "bf16x3 (fp32 in/out)",
+                    e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
+                    gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
+                    device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
+                    peaks=res["peak_kind"])
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/*
+ * gbpoly.h — C ABI of the GB300 (sm_103a) PolyBench dense-contraction library.
+ *
+ * This is the boundary that replaces the SYCL device queue of sycl-bench's
+ * polybench/{gemm,2mm,3mm,syrk,syr2k}.cpp.  Every entry point takes plain
+ * pointers and sizes, returns a gbpoly_status, and never throws.  Device
+ * pointers are opaque to the caller and owned by the caller.  A context is
+ * bound to one device and one CUDA stream; calls on one context are not
+ * thread-safe (the reference harness drives one queue from one thread,
+ * include/command_line.h:129-140).
+ *
+ * All matrices are dense and row-major: element (r, c) of a matrix with
+ * leading dimension ld lives at base[r * ld + c].  This is the layout of the
+ * reference's sycl::buffer<float, 2>(range<2>(N, N)) (polybench/gemm.cpp:69-71).
+ */
+#ifndef GBPOLY_H
+#define GBPOLY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  GBPOLY_OK is 0; everything else is an error whose text is
+ * returned by gbpoly_last_error().  The reference reports errors by throwing
+ * sycl::exception (include/common.h:208-212); the C++ harness turns a non-zero
+ * status back into an exception at the same place. */
+typedef enum {
+  GBPOLY_OK = 0,
+  GBPOLY_ERR_INVALID = 1,     /* bad argument (null pointer, negative size, bad enum) */
+  GBPOLY_ERR_CUDA = 2,        /* a CUDA runtime/driver call failed */
+  GBPOLY_ERR_NOMEM = 3,       /* device or pinned host allocation failed */
+  GBPOLY_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (kernel returned early) */
+  GBPOLY_ERR_UNSUPPORTED = 5, /* valid request this build or device cannot serve */
+  GBPOLY_ERR_STATE = 6        /* call out of order (e.g. graph end without begin) */
+} gbpoly_status;
+
+/* Arithmetic form of a contraction. */
+typedef enum {
+  GBPOLY_PREC_FP32 = 0,   /* plain FP32 SIMT FFMA kernels: the drop-in form */
+  GBPOLY_PREC_BF16X3 = 1, /* split-BF16: hi*hi + hi*lo + lo*hi on tcgen05, FP32 accumulation in TMEM */
+  GBPOLY_PREC_TF32 = 2,   /* tcgen05 kind::tf32, FP32 accumulation */
+  GBPOLY_PREC_FP8 = 3     /* e4m3 with one scale per 128x128 operand tile */
+} gbpoly_precision;
+
+/* Operand transposition: OP_N uses the matrix as stored, OP_T its transpose. */
+typedef enum { GBPOLY_OP_N = 0, GBPOLY_OP_T = 1 } gbpoly_op;
+
+typedef struct gbpoly_ctx gbpoly_ctx;
+
+/* ---------------------------------------------------------------- context -- */
+
+/* Create a context on CUDA device `device` with its own non-blocking stream.
+ * Replaces the queue construction of include/command_line.h:183-202. */
+gbpoly_status gbpoly_init(int device, gbpoly_ctx** out_ctx);
+
+/* Synchronise, release the context's workspace, stream and events. */
+gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx);
+
+/* Text of the last error on this thread ("" if none).  Valid until the next call. */
+const char* gbpoly_last_error(void);
+
+/* Device name, as the reference reads it with
+ * get_info<sycl::info::device::name>() (include/common.h:42-43). */
+gbpoly_status gbpoly_device_name(gbpoly_ctx* ctx, char* buf, size_t buflen);
+
+/* Number of SMs, current max SM clock (kHz) and compute capability. */
+gbpoly_status gbpoly_device_props(gbpoly_ctx* ctx, int* sm_count, int* sm_clock_khz, int* cc_major, int* cc_minor);
+
+/* Block until all work queued on the context's stream has finished, then
+ * report any device-side error word (a bounded wait that timed out).
+ * Replaces queue::wait_and_throw() (include/common.h:61, :75). */
+gbpoly_status gbpoly_synchronize(gbpoly_ctx* ctx);
+
+/* Use a caller-owned cudaStream_t (passed as void*) for all later work;
+ * NULL restores the context's own stream. */
+gbpoly_status gbpoly_set_stream(gbpoly_ctx* ctx, void* cuda_stream);
+
+/* ----------------------------------------------------------------- memory -- */
+
+/* Device buffers.  Together with gbpoly_memcpy_h2d they replace
+ * PrefetchedBuffer::initialize + forceDataTransfer (include/memory_wrappers.h:21-28, :47-51). */
+gbpoly_status gbpoly_malloc(gbpoly_ctx* ctx, void** dptr, size_t bytes);
+gbpoly_status gbpoly_free(gbpoly_ctx* ctx, void* dptr);
+
+/* Page-locked host buffers, for copies that overlap and run at full link speed. */
+gbpoly_status gbpoly_host_alloc(gbpoly_ctx* ctx, void** hptr, size_t bytes);
+gbpoly_status gbpoly_host_free(gbpoly_ctx* ctx, void* hptr);
+
+/* Copies are queued on the context's stream (asynchronous with respect to the
+ * host for pinned memory); gbpoly_synchronize() waits for them.  d2h replaces
+ * buffer::get_host_access() (polybench/gemm.cpp:99). */
+gbpoly_status gbpoly_memcpy_h2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes);
+gbpoly_status gbpoly_memcpy_d2h(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes);
+gbpoly_status gbpoly_memcpy_d2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes);
+gbpoly_status gbpoly_memset(gbpoly_ctx* ctx, void* dst, int value, size_t bytes);
+
+/* ----------------------------------------------------------------- events -- */
+
+/* Event handles for kernel-time profiling.  They replace the
+ * sycl::event profiling queries of include/common.h:88-96
+ * (command_start / command_end). */
+typedef struct gbpoly_event gbpoly_event;
+gbpoly_status gbpoly_event_create(gbpoly_ctx* ctx, gbpoly_event** ev);
+gbpoly_status gbpoly_event_destroy(gbpoly_ctx* ctx, gbpoly_event* ev);
+gbpoly_status gbpoly_event_record(gbpoly_ctx* ctx, gbpoly_event* ev);
+/* Milliseconds between two recorded events (waits for `end`). */
+gbpoly_status gbpoly_event_elapsed_ms(gbpoly_ctx* ctx, gbpoly_event* start, gbpoly_event* end, float* ms);
+
+/* ----------------------------------------------------------- contractions -- */
+
+/* C <- alpha * op(A) * op(B) + beta * C, FP32 in and out.
+ * op(A) is M x K, op(B) is K x N, C is M x N.
+ * Replaces the kernels polybench/gemm.cpp:82-91 (alpha=32412, beta=2123),
+ * polybench/2mm.cpp:99-106 (alpha=1, beta=1) and :114-122 (alpha=1, beta=0),
+ * polybench/3mm.cpp:120-157 (alpha=1, beta=1 onto zeroed E/F/G).
+ * With beta == 0, C is not read (NaN/Inf in C do not propagate).
+ * The call is asynchronous on the context's stream. */
+gbpoly_status gbpoly_gemm_f32(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op op_a, gbpoly_op op_b,
+    int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
+    float beta, float* C, int64_t ldc);
+
+/* C <- alpha * A * A^T + beta * C over the FULL N x N square (A is N x K).
+ * Replaces polybench/syrk.cpp:74-83 (alpha=123, beta=14512). */
+gbpoly_status gbpoly_syrk_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
+    const float* A, int64_t lda, float beta, float* C, int64_t ldc);
+
+/* C <- alpha * (A * B^T + B * A^T) + beta * C over the FULL N x N square
+ * (A, B are N x K), both products accumulated in one accumulator.
+ * Replaces polybench/syr2k.cpp:78-87 (alpha=1, beta=1). */
+gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
+    const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
+
+
+/* ------------------------------------------------------------------- FP64 -- */
+
+/* C <- alpha * op(A) * op(B) + beta * C in FP64.  The double variants of the
+ * benchmarks (the suite's SYCL_BENCH_HAS_FP64_SUPPORT idiom,
+ * single-kernel/nbody.cpp:303-309; polybench/gemm.cpp:14 fixes DATA_TYPE to
+ * float, so the reference itself has no double contraction) and the FP64
+ * oracle used for error norms at sizes the host loop cannot finish. */
+gbpoly_status gbpoly_gemm_f64(gbpoly_ctx* ctx, gbpoly_op op_a, gbpoly_op op_b, int64_t M, int64_t N, int64_t K,
+    double alpha, const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
+/* FP64 forms of gbpoly_syrk_f32 / gbpoly_syr2k_f32 (full square). */
+gbpoly_status gbpoly_syrk_f64(gbpoly_ctx* ctx, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+    double beta, double* C, int64_t ldc);
+gbpoly_status gbpoly_syr2k_f64(gbpoly_ctx* ctx, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+    const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
+
+/* dst[i] = (double)src[i] for i < count (device buffers). */
+gbpoly_status gbpoly_convert_f32_f64(gbpoly_ctx* ctx, const float* src, double* dst, int64_t count);
+
+/* Error of an FP32 result C against an FP64 reference R over a rows x cols
+ * window (device buffers).  Synchronous: waits for queued work, then returns
+ *   max_rel      = max|C-R| / max|R|
+ *   frob_rel     = ||C-R||_F / ||R||_F
+ *   max_elem_rel = max over R != 0 of |C-R| / |R|
+ * (+Inf for all three if any C-R is not finite).  This extends the
+ * reference's percentDiff verify (polybench/common/polybenchUtilFuncts.h:36-42),
+ * which it does not replace.  Any output pointer may be NULL. */
+gbpoly_status gbpoly_error_norms(gbpoly_ctx* ctx, const float* C, int64_t ldc, const double* R, int64_t ldr,
+    int64_t rows, int64_t cols, double* max_rel, double* frob_rel, double* max_elem_rel);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPOLY_H */

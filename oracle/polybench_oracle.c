@@ -1,0 +1,309 @@
+/*
+ * polybench_oracle.c — TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of sycl-bench's PolyBench dense-contraction benchmarks,
+ * used as the correctness oracle by the tests, by __graft_entry__.smoke()
+ * and by bench.py's CPU-baseline leg.  Nothing on the GPU product path links
+ * or calls this file.
+ *
+ * Every function follows one place of the reference (paths relative to the
+ * sycl-bench project root) and keeps its floating-point operation order:
+ *   - initialisers           polybench/gemm.cpp:18-40, 2mm.cpp:16-45,
+ *                            3mm.cpp:17-47, syrk.cpp:18-31, syr2k.cpp:18-32
+ *   - host reference loops   gemm.cpp:42-56, 2mm.cpp:47-69, 3mm.cpp:49-86,
+ *                            syrk.cpp:33-51, syr2k.cpp:34-52
+ *   - device kernel bodies   gemm.cpp:82-91, syrk.cpp:74-83, syr2k.cpp:78-87
+ *     (run on host cores: the reference's --device=cpu path)
+ *   - comparator             polybench/common/polybenchUtilFuncts.h:27-42
+ *
+ * Parallelism: OpenMP over output rows.  Each output element keeps the
+ * reference's sequential k order, so results do not depend on the thread
+ * count.  Build with -ffp-contract=off (no fused multiply-add) so the float
+ * operations are exactly the reference's mul-then-add on every host ISA.
+ *
+ * Pinned against the reference itself: oracle/build_ref.sh compiles the
+ * unmodified reference sources with a host-only SYCL shim, and
+ * tests/golden/make_golden.py stores their outputs; tests/test_oracle.py
+ * checks this file against those fixtures bit for bit.
+ */
+#include <math.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef long idx_t;
+
+/* ------------------------------------------------------------ comparator -- */
+
+/* polybenchUtilFuncts.h:27-33: absolute value of a float argument. */
+static float abs_val(float a) { return a < 0 ? a * -1 : a; }
+
+/* polybenchUtilFuncts.h:36-42.  Arguments are double, every absVal narrows to
+ * float, SMALL_FLOAT_VAL is 1e-8f added in double. */
+float orc_percent_diff(double v1, double v2) {
+  if(abs_val((float)v1) < 0.01 && abs_val((float)v2) < 0.01) return 0.0f;
+  return 100.0f * abs_val(abs_val((float)(v1 - v2)) / abs_val((float)(v1 + 0.00000001f)));
+}
+
+/* The verify loops (e.g. gemm.cpp:107-113): row-major walk, first element whose
+ * percentDiff exceeds `threshold` fails.  Returns that index or -1.  Also
+ * reports the largest percentDiff seen over the whole array in *max_diff and
+ * the number of failing elements in *n_fail (both extensions, for reporting). */
+idx_t orc_verify(const float* host, const float* dev, idx_t count, double threshold, float* max_diff, idx_t* n_fail) {
+  idx_t first = -1, fails = 0;
+  float worst = 0.0f;
+  for(idx_t i = 0; i < count; ++i) {
+    const float d = orc_percent_diff(host[i], dev[i]);
+    if(d > worst || d != d) worst = d;
+    if(d > threshold) {
+      if(first < 0) first = i;
+      ++fails;
+    }
+  }
+  if(max_diff) *max_diff = worst;
+  if(n_fail) *n_fail = fails;
+  return first;
+}
+
+/* -------------------------------------------------------------- initialisers */
+
+/* gemm.cpp:18-40 */
+void orc_gemm_init(float* A, float* B, float* C, idx_t n) {
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) A[i * n + j] = ((float)i * (float)j) / (float)n;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) B[i * n + j] = ((float)i * (float)j + 1) / (float)n;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) C[i * n + j] = ((float)i * (float)j + 2) / (float)n;
+}
+
+/* 2mm.cpp:16-45 (A, B, C, D; E is not initialised by the reference) */
+void orc_mm2_init(float* A, float* B, float* C, float* D, idx_t n) {
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) A[i * n + j] = ((float)i * (float)j) / (float)n;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) B[i * n + j] = ((float)i * (float)(j + 1)) / (float)n;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) C[i * n + j] = ((float)i * (float)(j + 3)) / (float)n;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) D[i * n + j] = ((float)i * (float)(j + 2)) / (float)n;
+}
+
+/* 3mm.cpp:17-47: same formulas as 2mm's four inputs. */
+void orc_mm3_init(float* A, float* B, float* C, float* D, idx_t n) { orc_mm2_init(A, B, C, D, n); }
+
+/* syrk.cpp:18-31 */
+void orc_syrk_init(float* A, float* C, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    for(idx_t j = 0; j < n; j++) A[i * n + j] = ((float)i * (float)j) / (float)n;
+    for(idx_t j = 0; j < n; j++) C[i * n + j] = ((float)i * (float)j + 2) / (float)n;
+  }
+}
+
+/* syr2k.cpp:18-32 */
+void orc_syr2k_init(float* A, float* B, float* C, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    for(idx_t j = 0; j < n; j++) C[i * n + j] = ((float)i * (float)j + 2) / (float)n;
+    for(idx_t j = 0; j < n; j++) {
+      A[i * n + j] = ((float)i * (float)j) / (float)n;
+      B[i * n + j] = ((float)i * (float)j + 1) / (float)n;
+    }
+  }
+}
+
+/* ------------------------------------------------------- host FP32 oracles -- */
+
+/* gemm.cpp:42-56, ALPHA=32412, BETA=2123 (int macros promoted to float). */
+void orc_gemm_host(const float* A, const float* B, float* C, idx_t n) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      C[i * n + j] *= 2123;
+      for(idx_t k = 0; k < n; ++k) C[i * n + j] += 32412 * A[i * n + k] * B[k * n + j];
+    }
+}
+
+/* 2mm.cpp:47-69: C += A.B in place, then E = C.D. */
+void orc_mm2_host(const float* A, const float* B, float* C, const float* D, float* E, idx_t n) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++)
+      for(idx_t k = 0; k < n; ++k) C[i * n + j] += A[i * n + k] * B[k * n + j];
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      E[i * n + j] = 0;
+      for(idx_t k = 0; k < n; ++k) E[i * n + j] += C[i * n + k] * D[k * n + j];
+    }
+}
+
+/* 3mm.cpp:49-86: E = A.B, F = C.D, G = E.F. */
+void orc_mm3_host(const float* A, const float* B, const float* C, const float* D, float* E, float* F, float* G,
+    idx_t n) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      E[i * n + j] = 0;
+      for(idx_t k = 0; k < n; ++k) E[i * n + j] += A[i * n + k] * B[k * n + j];
+    }
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      F[i * n + j] = 0;
+      for(idx_t k = 0; k < n; ++k) F[i * n + j] += C[i * n + k] * D[k * n + j];
+    }
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      G[i * n + j] = 0;
+      for(idx_t k = 0; k < n; ++k) G[i * n + j] += E[i * n + k] * F[k * n + j];
+    }
+}
+
+/* syrk.cpp:33-51, alpha=123, beta=14512 (float constants). */
+void orc_syrk_host(const float* A, float* C, idx_t n) {
+  const float alpha = 123, beta = 14512;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) C[i * n + j] *= beta;
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++)
+      for(idx_t k = 0; k < n; k++) C[i * n + j] += alpha * A[i * n + k] * A[j * n + k];
+}
+
+/* syr2k.cpp:34-52, ALPHA=BETA=1, two separate accumulations per k. */
+void orc_syr2k_host(const float* A, const float* B, float* C, idx_t n) {
+  const float alpha = 1, beta = 1;
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) C[i * n + j] *= beta;
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++)
+      for(idx_t k = 0; k < n; k++) {
+        C[i * n + j] += alpha * A[i * n + k] * B[j * n + k];
+        C[i * n + j] += alpha * B[i * n + k] * A[j * n + k];
+      }
+}
+
+/* ------------------------------------------- device kernel bodies on CPU -- */
+/* The reference's --device=cpu path runs each parallel_for body once per
+ * output element; a SYCL CPU runtime vectorises work-items along the
+ * innermost range dimension (j).  These restatements keep that shape: each
+ * element walks k in order (same result as one work-item), work-items are
+ * processed in blocks of kVec along j, rows [row_begin, row_end) only, so a
+ * bounded sample of the output can be timed. */
+enum { kVec = 64 };
+
+/* gemm.cpp:82-91: C[i][j] = BETA*C; C += ALPHA*A[i][k]*B[k][j].
+ * `alpha`, `beta` generalise the constants for the variant workloads. */
+void orc_gemm_body(const float* A, const float* B, float* C, idx_t n, idx_t row_begin, idx_t row_end, float alpha,
+    float beta) {
+  const idx_t nblk = (n + kVec - 1) / kVec;
+#pragma omp parallel for collapse(2) schedule(static)
+  for(idx_t i = row_begin; i < row_end; i++)
+    for(idx_t jb = 0; jb < nblk; jb++) {
+      const idx_t j0 = jb * kVec, j1 = (j0 + kVec < n) ? j0 + kVec : n;
+      float acc[kVec];
+      for(idx_t j = j0; j < j1; j++) acc[j - j0] = C[i * n + j] * beta;
+      for(idx_t k = 0; k < n; k++) {
+        const float a = alpha * A[i * n + k];
+        const float* b = B + k * n;
+        for(idx_t j = j0; j < j1; j++) acc[j - j0] += a * b[j];
+      }
+      for(idx_t j = j0; j < j1; j++) C[i * n + j] = acc[j - j0];
+    }
+}
+
+/* syrk.cpp:74-83: C = beta*C; C += alpha*A[i][k]*A[j][k]. */
+void orc_syrk_body(const float* A, float* C, idx_t n, idx_t row_begin, idx_t row_end, float alpha, float beta) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for(idx_t i = row_begin; i < row_end; i++)
+    for(idx_t j = 0; j < n; j++) {
+      float c = C[i * n + j] * beta;
+      for(idx_t k = 0; k < n; k++) c += alpha * A[i * n + k] * A[j * n + k];
+      C[i * n + j] = c;
+    }
+}
+
+/* syr2k.cpp:78-87: one statement per k, C += a*A_ik*B_jk + a*B_ik*A_jk. */
+void orc_syr2k_body(const float* A, const float* B, float* C, idx_t n, idx_t row_begin, idx_t row_end, float alpha,
+    float beta) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for(idx_t i = row_begin; i < row_end; i++)
+    for(idx_t j = 0; j < n; j++) {
+      float c = C[i * n + j] * beta;
+      for(idx_t k = 0; k < n; k++) c += alpha * A[i * n + k] * B[j * n + k] + alpha * B[i * n + k] * A[j * n + k];
+      C[i * n + j] = c;
+    }
+}
+
+/* ---------------------------------------------------------- FP64 oracles -- */
+
+/* out = alpha * op(A) op(B) + beta * C0 in double from FP32 operands,
+ * op(X) = X (op 0) or X^T (op 1), row-major with leading dimensions.
+ * C0 may be NULL (treated as zero).  `A2`,`B2` (may be NULL) add a second
+ * product op(A2) op(B2) with the same ops (syr2k). */
+void orc_gemm_f64(int op_a, int op_b, idx_t M, idx_t N, idx_t K, double alpha, const float* A, idx_t lda,
+    const float* B, idx_t ldb, const float* A2, const float* B2, double beta, const float* C0, idx_t ldc,
+    double* out, idx_t ldo) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < M; i++) {
+    for(idx_t j = 0; j < N; j++) {
+      double s = 0.0;
+      for(idx_t k = 0; k < K; k++) {
+        const double a = op_a ? A[k * lda + i] : A[i * lda + k];
+        const double b = op_b ? B[j * ldb + k] : B[k * ldb + j];
+        s += a * b;
+        if(A2 && B2) {
+          const double a2 = op_a ? A2[k * lda + i] : A2[i * lda + k];
+          const double b2 = op_b ? B2[j * ldb + k] : B2[k * ldb + j];
+          s += a2 * b2;
+        }
+      }
+      out[i * ldo + j] = alpha * s + (C0 ? beta * (double)C0[i * ldc + j] : 0.0);
+    }
+  }
+}
+
+/* Same as orc_gemm_f64 with double operands (chained stages of 2mm/3mm). */
+void orc_gemm_f64d(idx_t M, idx_t N, idx_t K, double alpha, const double* A, idx_t lda, const double* B, idx_t ldb,
+    double beta, const double* C0, idx_t ldc, double* out, idx_t ldo) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < M; i++)
+    for(idx_t j = 0; j < N; j++) {
+      double s = 0.0;
+      for(idx_t k = 0; k < K; k++) s += A[i * lda + k] * B[k * ldb + j];
+      out[i * ldo + j] = alpha * s + (C0 ? beta * C0[i * ldc + j] : 0.0);
+    }
+}
+
+/* Normwise error of an FP32 result against an FP64 reference:
+ *   max_rel  = max|C - R| / max|R|,   frob_rel = ||C - R||_F / ||R||_F.
+ * Elementwise relative error max(|C-R|/|R|) over |R| > 0 also reported. */
+void orc_error_norms(const float* C, const double* R, idx_t count, double* max_rel, double* frob_rel,
+    double* max_elem_rel) {
+  double max_err = 0, max_ref = 0, se = 0, sr = 0, mer = 0;
+  for(idx_t i = 0; i < count; i++) {
+    const double e = fabs((double)C[i] - R[i]);
+    const double r = fabs(R[i]);
+    if(e > max_err || e != e) max_err = e;
+    if(r > max_ref) max_ref = r;
+    se += e * e;
+    sr += r * r;
+    if(r > 0 && e / r > mer) mer = e / r;
+  }
+  if(max_rel) *max_rel = max_ref > 0 ? max_err / max_ref : max_err;
+  if(frob_rel) *frob_rel = sr > 0 ? sqrt(se / sr) : sqrt(se);
+  if(max_elem_rel) *max_elem_rel = mer;
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

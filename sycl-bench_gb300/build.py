@@ -1,0 +1,124 @@
+"""Build libgbpoly.so (CUDA, sm_103a) and the PolyBench executables in-tree.
+
+    python sycl-bench_gb300/build.py            # library + executables
+    python sycl-bench_gb300/build.py --lib      # library only
+
+Outputs (git-ignored):
+    sycl-bench_gb300/lib/libgbpoly.so
+    sycl-bench_gb300/bin/polybench_{gemm,2mm,3mm,syrk,syr2k}
+
+Translation units compile in parallel; a unit is rebuilt only when it or a
+header it may include is newer than its object.  Host code is portable C++17
+(the GPU machine is aarch64, this build also runs on x86_64).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+HARNESS = PKG / "harness"
+POLY = PKG / "polybench"
+LIB_DIR = PKG / "lib"
+BIN_DIR = PKG / "bin"
+OBJ_DIR = PKG / "_build"
+INCLUDE = ROOT / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-Xptxas", "-warn-spills"] + ARCH
+CXX_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-Wall", "-Wno-unknown-pragmas"]
+
+BENCHMARKS = ["gemm", "2mm", "3mm", "syrk", "syr2k"]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found")
+    return cand
+
+
+def cuda_home() -> Path:
+    return Path(nvcc()).resolve().parent.parent
+
+
+def _newer(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps if d.exists())
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if r.stderr.strip():
+        # ptxas spill warnings and the like: keep them visible
+        sys.stderr.write(r.stderr)
+
+
+def build_lib(verbose: bool = False) -> Path:
+    OBJ_DIR.mkdir(exist_ok=True)
+    LIB_DIR.mkdir(exist_ok=True)
+    sources = sorted(CSRC.glob("*.cu"))
+    headers = sorted(CSRC.glob("*.cuh")) + [INCLUDE / "gbpoly.h"]
+    jobs = []
+    objs = []
+    for src in sources:
+        obj = OBJ_DIR / (src.stem + ".o")
+        objs.append(obj)
+        if _newer(obj, [src] + headers):
+            cmd = [nvcc(), *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+            if verbose:
+                cmd += ["-Xptxas", "-v"]
+            jobs.append(cmd)
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(_run, jobs))
+    lib = LIB_DIR / "libgbpoly.so"
+    if jobs or _newer(lib, objs):
+        _run([nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"])
+    return lib
+
+
+def build_executables() -> list[Path]:
+    BIN_DIR.mkdir(exist_ok=True)
+    lib = LIB_DIR / "libgbpoly.so"
+    cuda_inc = cuda_home() / "include"
+    headers = sorted(HARNESS.glob("*.h")) + sorted(POLY.glob("*.h")) + [INCLUDE / "gbpoly.h", lib]
+    jobs, outs = [], []
+    for name in BENCHMARKS:
+        src = POLY / f"{name}.cpp"
+        out = BIN_DIR / f"polybench_{name}"
+        outs.append(out)
+        if _newer(out, [src] + headers):
+            jobs.append([shutil.which("g++") or "g++", *CXX_FLAGS, "-I", str(HARNESS), "-I", str(POLY),
+                         "-I", str(INCLUDE), "-I", str(cuda_inc), str(src), "-o", str(out),
+                         "-L", str(LIB_DIR), "-lgbpoly", f"-Wl,-rpath,{LIB_DIR}", "-Wl,-rpath,$ORIGIN/../lib"])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(_run, jobs))
+    return outs
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--lib", action="store_true", help="library only")
+    ap.add_argument("-v", "--verbose", action="store_true", help="ptxas resource usage")
+    args = ap.parse_args()
+    lib = build_lib(verbose=args.verbose)
+    print(lib)
+    if not args.lib and (POLY / "gemm.cpp").exists():
+        for p in build_executables():
+            print(p)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,328 @@
+// C ABI of libgbpoly: context, memory, events and the contraction entry
+// points declared in include/gbpoly.h.  Argument checking lives here; the
+// kernels live in their own translation units.
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+
+#include "gbpoly_internal.cuh"
+
+namespace gbpoly {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+gbpoly_status fail(gbpoly_status code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+gbpoly_status cuda_fail(cudaError_t e, const char* what) {
+  std::string msg = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  set_error(msg);
+  return (e == cudaErrorMemoryAllocation) ? GBPOLY_ERR_NOMEM : GBPOLY_ERR_CUDA;
+}
+
+gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) {
+  if(ctx->ws.bytes >= bytes) return GBPOLY_OK;
+  if(ctx->ws.ptr) {
+    GBPOLY_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    GBPOLY_CUDA_TRY(cudaFree(ctx->ws.ptr));
+    ctx->ws.ptr = nullptr;
+    ctx->ws.bytes = 0;
+  }
+  const size_t rounded = (bytes + (size_t(1) << 21) - 1) & ~((size_t(1) << 21) - 1);
+  GBPOLY_CUDA_TRY(cudaMalloc(&ctx->ws.ptr, rounded));
+  ctx->ws.bytes = rounded;
+  return GBPOLY_OK;
+}
+
+gbpoly_status make_tmap_2d(gbpoly_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dtype, size_t elem_bytes,
+    const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols,
+    CUtensorMapSwizzle swizzle) {
+  if(!ctx->encode_tiled) return fail(GBPOLY_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {ld * elem_bytes};
+  const cuuint32_t box[2] = {box_cols, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = ctx->encode_tiled(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if(r != CUDA_SUCCESS) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+        "cuTensorMapEncodeTiled failed (%d): rows=%llu cols=%llu ld=%llu box=%ux%u elem=%zu base=%p", int(r),
+        (unsigned long long)rows, (unsigned long long)cols, (unsigned long long)ld, box_rows, box_cols, elem_bytes,
+        base);
+    return fail(GBPOLY_ERR_INVALID, buf);
+  }
+  return GBPOLY_OK;
+}
+
+}  // namespace gbpoly
+
+using namespace gbpoly;
+
+namespace {
+
+gbpoly_status check_ctx(gbpoly_ctx* ctx) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if(e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return GBPOLY_OK;
+}
+
+#define CTX_TRY(ctx)                               \
+  do {                                             \
+    gbpoly_status _s = check_ctx(ctx);             \
+    if(_s != GBPOLY_OK) return _s;                 \
+  } while(0)
+
+gbpoly_status check_matrix(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld) {
+  if(rows < 0 || cols < 0) return fail(GBPOLY_ERR_INVALID, std::string(name) + ": negative dimension");
+  if(rows > 0 && cols > 0) {
+    if(!p) return fail(GBPOLY_ERR_INVALID, std::string(name) + ": null pointer");
+    if(ld < cols) return fail(GBPOLY_ERR_INVALID, std::string(name) + ": leading dimension smaller than columns");
+  }
+  return GBPOLY_OK;
+}
+
+}  // namespace
+
+struct gbpoly_event {
+  cudaEvent_t ev = nullptr;
+};
+
+extern "C" {
+
+const char* gbpoly_last_error(void) { return last_error_cstr(); }
+
+gbpoly_status gbpoly_init(int device, gbpoly_ctx** out_ctx) {
+  if(!out_ctx) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  *out_ctx = nullptr;
+  int count = 0;
+  GBPOLY_CUDA_TRY(cudaGetDeviceCount(&count));
+  if(device < 0 || device >= count) return fail(GBPOLY_ERR_INVALID, "device index out of range");
+  GBPOLY_CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  GBPOLY_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  auto* ctx = new gbpoly_ctx();
+  ctx->device = device;
+  ctx->sm_count = prop.multiProcessorCount;
+  int clk = 0;
+  cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
+  ctx->sm_clock_khz = clk;
+  ctx->cc_major = prop.major;
+  ctx->cc_minor = prop.minor;
+  strncpy(ctx->name, prop.name, sizeof(ctx->name) - 1);
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if(e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->err_host), sizeof(int), cudaHostAllocMapped);
+  if(e == cudaSuccess) {
+    *ctx->err_host = 0;
+    e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->err_dev), ctx->err_host, 0);
+  }
+  if(e != cudaSuccess) {
+    gbpoly_status st = cuda_fail(e, "context setup");
+    if(ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if(ctx->err_host) cudaFreeHost(ctx->err_host);
+    delete ctx;
+    return st;
+  }
+  ctx->stream = ctx->own_stream;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    ctx->encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  *out_ctx = ctx;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
+  if(!ctx) return GBPOLY_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if(ctx->ws.ptr) cudaFree(ctx->ws.ptr);
+  if(ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  if(ctx->err_host) cudaFreeHost(ctx->err_host);
+  delete ctx;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_device_name(gbpoly_ctx* ctx, char* buf, size_t buflen) {
+  if(!ctx || !buf || buflen == 0) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  strncpy(buf, ctx->name, buflen - 1);
+  buf[buflen - 1] = 0;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_device_props(gbpoly_ctx* ctx, int* sm_count, int* sm_clock_khz, int* cc_major, int* cc_minor) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  if(sm_count) *sm_count = ctx->sm_count;
+  if(sm_clock_khz) *sm_clock_khz = ctx->sm_clock_khz;
+  if(cc_major) *cc_major = ctx->cc_major;
+  if(cc_minor) *cc_minor = ctx->cc_minor;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_synchronize(gbpoly_ctx* ctx) {
+  CTX_TRY(ctx);
+  GBPOLY_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  const int code = *reinterpret_cast<volatile int*>(ctx->err_host);
+  if(code != 0) {
+    *reinterpret_cast<volatile int*>(ctx->err_host) = 0;
+    char buf[160];
+    snprintf(buf, sizeof buf, "a device-side bounded wait timed out (code %d); the kernel returned early", code);
+    return fail(GBPOLY_ERR_TIMEOUT, buf);
+  }
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_set_stream(gbpoly_ctx* ctx, void* cuda_stream) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  ctx->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : ctx->own_stream;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_malloc(gbpoly_ctx* ctx, void** dptr, size_t bytes) {
+  CTX_TRY(ctx);
+  if(!dptr) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  *dptr = nullptr;
+  if(bytes == 0) return GBPOLY_OK;
+  GBPOLY_CUDA_TRY(cudaMalloc(dptr, bytes));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_free(gbpoly_ctx* ctx, void* dptr) {
+  CTX_TRY(ctx);
+  if(dptr) GBPOLY_CUDA_TRY(cudaFree(dptr));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_host_alloc(gbpoly_ctx* ctx, void** hptr, size_t bytes) {
+  CTX_TRY(ctx);
+  if(!hptr) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  *hptr = nullptr;
+  if(bytes == 0) return GBPOLY_OK;
+  GBPOLY_CUDA_TRY(cudaHostAlloc(hptr, bytes, cudaHostAllocDefault));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_host_free(gbpoly_ctx* ctx, void* hptr) {
+  CTX_TRY(ctx);
+  if(hptr) GBPOLY_CUDA_TRY(cudaFreeHost(hptr));
+  return GBPOLY_OK;
+}
+
+static gbpoly_status copy(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+  CTX_TRY(ctx);
+  if(bytes == 0) return GBPOLY_OK;
+  if(!dst || !src) return fail(GBPOLY_ERR_INVALID, "null copy pointer");
+  GBPOLY_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_memcpy_h2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  return copy(ctx, dst, src, bytes, cudaMemcpyHostToDevice);
+}
+gbpoly_status gbpoly_memcpy_d2h(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  return copy(ctx, dst, src, bytes, cudaMemcpyDeviceToHost);
+}
+gbpoly_status gbpoly_memcpy_d2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  return copy(ctx, dst, src, bytes, cudaMemcpyDeviceToDevice);
+}
+
+gbpoly_status gbpoly_memset(gbpoly_ctx* ctx, void* dst, int value, size_t bytes) {
+  CTX_TRY(ctx);
+  if(bytes == 0) return GBPOLY_OK;
+  if(!dst) return fail(GBPOLY_ERR_INVALID, "null pointer");
+  GBPOLY_CUDA_TRY(cudaMemsetAsync(dst, value, bytes, ctx->stream));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_event_create(gbpoly_ctx* ctx, gbpoly_event** ev) {
+  CTX_TRY(ctx);
+  if(!ev) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  auto* e = new gbpoly_event();
+  cudaError_t r = cudaEventCreate(&e->ev);
+  if(r != cudaSuccess) {
+    delete e;
+    return cuda_fail(r, "cudaEventCreate");
+  }
+  *ev = e;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_event_destroy(gbpoly_ctx* ctx, gbpoly_event* ev) {
+  CTX_TRY(ctx);
+  if(ev) {
+    cudaEventDestroy(ev->ev);
+    delete ev;
+  }
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_event_record(gbpoly_ctx* ctx, gbpoly_event* ev) {
+  CTX_TRY(ctx);
+  if(!ev) return fail(GBPOLY_ERR_INVALID, "null event");
+  GBPOLY_CUDA_TRY(cudaEventRecord(ev->ev, ctx->stream));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_event_elapsed_ms(gbpoly_ctx* ctx, gbpoly_event* start, gbpoly_event* end, float* ms) {
+  CTX_TRY(ctx);
+  if(!start || !end || !ms) return fail(GBPOLY_ERR_INVALID, "null argument");
+  GBPOLY_CUDA_TRY(cudaEventSynchronize(end->ev));
+  GBPOLY_CUDA_TRY(cudaEventElapsedTime(ms, start->ev, end->ev));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_gemm_f32(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op op_a, gbpoly_op op_b, int64_t M,
+    int64_t N, int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb, float beta,
+    float* C, int64_t ldc) {
+  CTX_TRY(ctx);
+  if((op_a != GBPOLY_OP_N && op_a != GBPOLY_OP_T) || (op_b != GBPOLY_OP_N && op_b != GBPOLY_OP_T))
+    return fail(GBPOLY_ERR_INVALID, "bad operand op");
+  if(M < 0 || N < 0 || K < 0) return fail(GBPOLY_ERR_INVALID, "negative dimension");
+  gbpoly_status st;
+  if((st = check_matrix("A", A, op_a == GBPOLY_OP_N ? M : K, op_a == GBPOLY_OP_N ? K : M, lda)) != GBPOLY_OK) return st;
+  if((st = check_matrix("B", B, op_b == GBPOLY_OP_N ? K : N, op_b == GBPOLY_OP_N ? N : K, ldb)) != GBPOLY_OK) return st;
+  if((st = check_matrix("C", C, M, N, ldc)) != GBPOLY_OK) return st;
+  GemmF32Args a{};
+  a.M = M, a.N = N, a.K = K, a.alpha = alpha, a.beta = beta, a.op_a = op_a, a.op_b = op_b;
+  a.A = A, a.lda = lda, a.B = B, a.ldb = ldb, a.C = C, a.ldc = ldc;
+  switch(prec) {
+  case GBPOLY_PREC_FP32: return launch_gemm_f32_simt(ctx, a);
+  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
+  }
+}
+
+gbpoly_status gbpoly_syrk_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
+    const float* A, int64_t lda, float beta, float* C, int64_t ldc) {
+  return gbpoly_gemm_f32(ctx, prec, GBPOLY_OP_N, GBPOLY_OP_T, N, N, K, alpha, A, lda, A, lda, beta, C, ldc);
+}
+
+gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
+    const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc) {
+  CTX_TRY(ctx);
+  gbpoly_status st;
+  if(N < 0 || K < 0) return fail(GBPOLY_ERR_INVALID, "negative dimension");
+  if((st = check_matrix("A", A, N, K, lda)) != GBPOLY_OK) return st;
+  if((st = check_matrix("B", B, N, K, ldb)) != GBPOLY_OK) return st;
+  if((st = check_matrix("C", C, N, N, ldc)) != GBPOLY_OK) return st;
+  GemmF32Args a{};
+  a.M = N, a.N = N, a.K = K, a.alpha = alpha, a.beta = beta, a.op_a = GBPOLY_OP_N, a.op_b = GBPOLY_OP_T;
+  a.A = A, a.lda = lda, a.B = B, a.ldb = ldb, a.C = C, a.ldc = ldc;
+  a.dual = true, a.A2 = B, a.lda2 = ldb, a.B2 = A, a.ldb2 = lda;
+  switch(prec) {
+  case GBPOLY_PREC_FP32: return launch_gemm_f32_simt(ctx, a);
+  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
+  }
+}
+
+}  // extern "C"

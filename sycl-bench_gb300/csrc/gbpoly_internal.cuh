@@ -1,0 +1,175 @@
+// Internal declarations shared by the gbpoly CUDA translation units.
+//
+// Device helpers here are hand-written inline PTX for sm_103a: mbarrier
+// phases with bounded waits, 2-D TMA tile loads, and the global timer.
+// Every wait on an mbarrier gives up after kWaitTimeoutNs, records a code in
+// the context's error word (mapped host memory) and lets the kernel return,
+// so a broken pipeline never hangs the GPU.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gbpoly.h"
+
+namespace gbpoly {
+
+// ------------------------------------------------------------------ host side
+
+// Error word codes written by kernels (first writer wins).
+enum DeviceError : int {
+  kDevErrNone = 0,
+  kDevErrFullWait = 1,    // consumer waited too long for a filled stage
+  kDevErrEmptyWait = 2,   // producer waited too long for a drained stage
+  kDevErrMmaWait = 3,     // epilogue waited too long for the accumulator
+  kDevErrDrainWait = 4,   // teardown waited too long for in-flight copies
+  kDevErrTmemAlloc = 5,   // tensor-memory allocation did not fit
+};
+
+struct Workspace {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace gbpoly
+
+struct gbpoly_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int* err_host = nullptr;  // mapped pinned word; kernels write it, host reads after sync
+  int* err_dev = nullptr;   // device alias of err_host
+  int sm_count = 0;
+  int sm_clock_khz = 0;
+  int cc_major = 0, cc_minor = 0;
+  char name[256] = {0};
+  gbpoly::Workspace ws;
+  PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
+};
+
+namespace gbpoly {
+
+// Thread-local error text, returned by gbpoly_last_error().
+void set_error(const std::string& msg);
+gbpoly_status fail(gbpoly_status code, const std::string& msg);
+gbpoly_status cuda_fail(cudaError_t e, const char* what);
+
+#define GBPOLY_CUDA_TRY(expr)                                  \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if(_e != cudaSuccess) return ::gbpoly::cuda_fail(_e, #expr); \
+  } while(0)
+
+// Grow the context workspace to at least `bytes` (synchronises when it grows).
+gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes);
+
+// 2-D tensor map over a row-major matrix of `rows` x `cols` elements with
+// leading dimension `ld` (elements), box `box_rows` x `box_cols`.
+gbpoly_status make_tmap_2d(gbpoly_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dtype, size_t elem_bytes,
+    const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols,
+    CUtensorMapSwizzle swizzle);
+
+// FP32 SIMT entry points (sgemm_simt.cu).
+struct GemmF32Args {
+  int64_t M, N, K;
+  float alpha, beta;
+  gbpoly_op op_a, op_b;
+  const float* A;
+  int64_t lda;
+  const float* B;
+  int64_t ldb;
+  float* C;
+  int64_t ldc;
+  // Second product accumulated into the same C (syr2k): A2 (N x K) times B2^T.
+  bool dual = false;
+  const float* A2 = nullptr;
+  int64_t lda2 = 0;
+  const float* B2 = nullptr;
+  int64_t ldb2 = 0;
+};
+gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
+
+// ---------------------------------------------------------------- device side
+
+constexpr unsigned long long kWaitTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for phase `parity` of `bar` to complete.  Returns false (after
+// recording `code` in *err) if it does not within kWaitTimeoutNs, or as soon
+// as another thread of the grid has recorded an error.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  if(mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while(true) {
+#pragma unroll 1
+    for(int i = 0; i < 32; ++i)
+      if(mbar_try_wait(bar, parity)) return true;
+    if(*reinterpret_cast<volatile int*>(err) != 0) return false;
+    if(global_timer_ns() - t0 > kWaitTimeoutNs) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// 2-D tiled TMA load: box at (x = innermost coordinate, y) into smem `dst`,
+// completion signalled as transaction bytes on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+}  // namespace gbpoly

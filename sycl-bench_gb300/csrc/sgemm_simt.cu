@@ -1,0 +1,313 @@
+// Plain FP32 SIMT contraction kernels for sm_103a: the drop-in form of the
+// PolyBench kernels polybench/gemm.cpp:82-91, 2mm.cpp:99-122, 3mm.cpp:120-157,
+// syrk.cpp:74-83 and syr2k.cpp:78-87.
+//
+// The reference launches one work-item per C element that walks the whole k
+// range through global memory.  Here one CTA owns a 128x128 tile of C:
+//   * one producer warp streams BK=32 slices of the A and B panels into a
+//     ring of shared-memory stages with 2-D TMA (cp.async.bulk.tensor),
+//     each stage guarded by a full/empty mbarrier pair;
+//   * eight consumer warps (256 threads) each keep an 8x8 block of C in
+//     registers and run FFMA over 128-bit shared-memory loads;
+//   * the epilogue applies C = alpha*acc + beta*C with bounds checks.
+// syr2k's two products (A_i.B_j + B_i.A_j) stream four tiles per stage into
+// the same accumulator.  Operands whose base or leading dimension is not
+// 16-byte aligned (TMA's rule) take a simple tiled kernel without TMA.
+#include "gbpoly_internal.cuh"
+#include "tiled_gemm.cuh"
+
+namespace gbpoly {
+namespace {
+
+constexpr int kBM = 128, kBN = 128, kBK = 32;
+constexpr int kConsumers = 256;            // 8 consumer warps
+constexpr int kThreads = kConsumers + 32;  // + 1 producer warp
+constexpr int kTileBytes = kBM * kBK * 4;  // 16 KB, same for every tile shape used
+
+// Byte offset of float4 chunk `chunk` (0..7) of row `row` in a [rows][32]
+// fp32 tile written by TMA with 128-byte swizzle (chunk index XOR row%8).
+__device__ __forceinline__ uint32_t swz128(int row, int chunk) {
+  return static_cast<uint32_t>(row * 128 + ((chunk ^ (row & 7)) << 4));
+}
+
+// Operand tile layouts in shared memory:
+//  K-major (k innermost, e.g. A as stored, or B^T as stored):
+//     [128 rows][32 k], 128-byte swizzled.
+//  MN-major (row/col innermost, e.g. B as stored for C = A.B):
+//     [32 k][128], unswizzled 512-byte rows.
+//
+// Register fragment: v[i][kk] for the 8 rows (or columns) this thread owns
+// and the 4 k values of one k-step.
+//  MN-major: owned indices 4t..4t+3 and 64+4t..64+4t+3 (vector loads along the row).
+//  K-major:  owned indices t+16i (rows t, t+16, ...), so that the 8 lanes of a
+//            quarter warp hit 8 distinct swizzle phases (conflict-free).
+template <bool KMAJ>
+__device__ __forceinline__ int owned_index(int t, int i) {
+  if constexpr(KMAJ)
+    return t + 16 * i;
+  else
+    return (i < 4) ? (4 * t + i) : (64 + 4 * t + (i - 4));
+}
+
+template <bool KMAJ>
+__device__ __forceinline__ void load_frag(const char* tile, int t, int kstep, float (&v)[8][4]) {
+  if constexpr(KMAJ) {
+#pragma unroll
+    for(int i = 0; i < 8; ++i) {
+      const int row = t + 16 * i;
+      const float4 x = *reinterpret_cast<const float4*>(tile + swz128(row, kstep));
+      v[i][0] = x.x;
+      v[i][1] = x.y;
+      v[i][2] = x.z;
+      v[i][3] = x.w;
+    }
+  } else {
+#pragma unroll
+    for(int kk = 0; kk < 4; ++kk) {
+      const char* rowp = tile + (kstep * 4 + kk) * 512;
+      const float4 lo = *reinterpret_cast<const float4*>(rowp + 16 * t);
+      const float4 hi = *reinterpret_cast<const float4*>(rowp + 256 + 16 * t);
+      v[0][kk] = lo.x;
+      v[1][kk] = lo.y;
+      v[2][kk] = lo.z;
+      v[3][kk] = lo.w;
+      v[4][kk] = hi.x;
+      v[5][kk] = hi.y;
+      v[6][kk] = hi.z;
+      v[7][kk] = hi.w;
+    }
+  }
+}
+
+template <bool A_KMAJ, bool B_KMAJ>
+__device__ __forceinline__ void mma_tile(const char* ta, const char* tb, int tm, int tn, float (&acc)[8][8]) {
+#pragma unroll 1
+  for(int ks = 0; ks < kBK / 4; ++ks) {
+    float a[8][4], b[8][4];
+    load_frag<A_KMAJ>(ta, tm, ks, a);
+    load_frag<B_KMAJ>(tb, tn, ks, b);
+#pragma unroll
+    for(int kk = 0; kk < 4; ++kk)
+#pragma unroll
+      for(int i = 0; i < 8; ++i)
+#pragma unroll
+        for(int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i][kk], b[j][kk], acc[i][j]);
+  }
+}
+
+// Tile rasterisation: groups of 8 tile-rows walk the tile-columns together so
+// that concurrently resident CTAs share A and B panels in L2.
+__device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, int& tile_m, int& tile_n) {
+  constexpr int G = 8;
+  const int per_group = G * tiles_n;
+  const int group = id / per_group;
+  const int first = group * G;
+  const int gsz = min(tiles_m - first, G);
+  const int r = id - group * per_group;
+  tile_m = first + r % gsz;
+  tile_n = r / gsz;
+}
+
+// A_KMAJ: op(A) rows are contiguous in k (op_a == N).  B_KMAJ: op(B) columns
+// are contiguous in k (op_b == T).  DUAL: syr2k, tiles A_i, B_j, B_i, A_j.
+template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
+__global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+    const __grid_constant__ CUtensorMap tmB, int M, int N, int K, float alpha, float beta, float* __restrict__ C,
+    int64_t ldc, int* err) {
+  constexpr int kTilesPerStage = DUAL ? 4 : 2;
+  constexpr int kStageBytes = kTilesPerStage * kTileBytes;
+  extern __shared__ __align__(1024) char smem_raw[];
+  // 1024-byte aligned (128-byte swizzle atoms); offset arithmetic keeps the pointer in the shared window
+  char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * kStageBytes);
+  uint64_t* empty = full + STAGES;
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int tiles_m = (M + kBM - 1) / kBM, tiles_n = (N + kBN - 1) / kBN;
+  int tile_m, tile_n;
+  tile_coords(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
+  const int m0 = tile_m * kBM, n0 = tile_n * kBN;
+  const int ktiles = (K + kBK - 1) / kBK;
+
+  if(tid == 0) {
+#pragma unroll
+    for(int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumers / 32);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  if(warp == kConsumers / 32) {
+    // ------------------------------------------------------------ producer
+    if(lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      int issued = 0;
+      for(int kt = 0; kt < ktiles; ++kt) {
+        const int s = kt % STAGES;
+        if(kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, err, kDevErrEmptyWait)) break;
+        char* st = smem + s * kStageBytes;
+        mbar_arrive_expect_tx(&full[s], kStageBytes);
+        const int k0 = kt * kBK;
+        if constexpr(DUAL) {
+          tma_load_2d(st + 0 * kTileBytes, &tmA, &full[s], k0, m0);  // A rows of the C tile
+          tma_load_2d(st + 1 * kTileBytes, &tmB, &full[s], k0, n0);  // B rows of the C tile columns
+          tma_load_2d(st + 2 * kTileBytes, &tmB, &full[s], k0, m0);
+          tma_load_2d(st + 3 * kTileBytes, &tmA, &full[s], k0, n0);
+        } else {
+          if constexpr(A_KMAJ)
+            tma_load_2d(st, &tmA, &full[s], k0, m0);
+          else
+            tma_load_2d(st, &tmA, &full[s], m0, k0);
+          if constexpr(B_KMAJ)
+            tma_load_2d(st + kTileBytes, &tmB, &full[s], k0, n0);
+          else
+            tma_load_2d(st + kTileBytes, &tmB, &full[s], n0, k0);
+        }
+        ++issued;
+      }
+      // Drain: do not leave the CTA while copies into its shared memory are in flight.
+      for(int kt = max(0, issued - STAGES); kt < issued; ++kt) {
+        if(!mbar_wait(&full[kt % STAGES], (kt / STAGES) & 1, err, kDevErrDrainWait)) break;
+      }
+    }
+    return;
+  }
+
+  // -------------------------------------------------------------- consumers
+  const int tm = warp * 2 + (lane >> 4);  // 0..15
+  const int tn = lane & 15;               // 0..15
+  float acc[8][8];
+#pragma unroll
+  for(int i = 0; i < 8; ++i)
+#pragma unroll
+    for(int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  bool ok = true;
+  for(int kt = 0; kt < ktiles; ++kt) {
+    const int s = kt % STAGES;
+    if(!mbar_wait(&full[s], (kt / STAGES) & 1, err, kDevErrFullWait)) {
+      ok = false;
+      break;
+    }
+    const char* st = smem + s * kStageBytes;
+    if constexpr(DUAL) {
+      mma_tile<true, true>(st + 0 * kTileBytes, st + 1 * kTileBytes, tm, tn, acc);
+      mma_tile<true, true>(st + 2 * kTileBytes, st + 3 * kTileBytes, tm, tn, acc);
+    } else {
+      mma_tile<A_KMAJ, B_KMAJ>(st, st + kTileBytes, tm, tn, acc);
+    }
+    __syncwarp();
+    if(lane == 0) mbar_arrive(&empty[s]);
+  }
+  if(!ok) return;
+
+  // --------------------------------------------------------------- epilogue
+  constexpr bool kVecCols = !B_KMAJ && !DUAL;
+  const bool vec_ok = kVecCols && ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+#pragma unroll
+  for(int i = 0; i < 8; ++i) {
+    const int m = m0 + owned_index<A_KMAJ || DUAL>(tm, i);
+    if(m >= M) continue;
+    float* crow = C + static_cast<int64_t>(m) * ldc;
+    if(vec_ok) {
+#pragma unroll
+      for(int h = 0; h < 2; ++h) {
+        const int n = n0 + h * 64 + 4 * tn;
+        if(n + 3 < N) {
+          float4 out = make_float4(alpha * acc[i][4 * h + 0], alpha * acc[i][4 * h + 1], alpha * acc[i][4 * h + 2],
+              alpha * acc[i][4 * h + 3]);
+          if(beta != 0.f) {
+            const float4 c = *reinterpret_cast<const float4*>(crow + n);
+            out.x = fmaf(beta, c.x, out.x);
+            out.y = fmaf(beta, c.y, out.y);
+            out.z = fmaf(beta, c.z, out.z);
+            out.w = fmaf(beta, c.w, out.w);
+          }
+          *reinterpret_cast<float4*>(crow + n) = out;
+          continue;
+        }
+#pragma unroll
+        for(int q = 0; q < 4; ++q) {
+          if(n + q < N) {
+            const float v = alpha * acc[i][4 * h + q];
+            crow[n + q] = (beta != 0.f) ? fmaf(beta, crow[n + q], v) : v;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for(int j = 0; j < 8; ++j) {
+        const int n = n0 + owned_index<B_KMAJ || DUAL>(tn, j);
+        if(n < N) {
+          const float v = alpha * acc[i][j];
+          crow[n] = (beta != 0.f) ? fmaf(beta, crow[n], v) : v;
+        }
+      }
+    }
+  }
+}
+
+template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
+gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMap& ta, const CUtensorMap& tb) {
+  constexpr int kStageBytes = (DUAL ? 4 : 2) * kTileBytes;
+  constexpr int kSmem = STAGES * kStageBytes + 1024 + 2 * STAGES * 8;
+  auto kern = sgemm_tma_kernel<A_KMAJ, B_KMAJ, DUAL, STAGES>;
+  static unsigned attr_set = 0;  // one bit per device: the attribute is set once per device
+  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
+    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem));
+    attr_set |= 1u << ctx->device;
+  }
+  const int64_t tiles = ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN);
+  kern<<<static_cast<unsigned>(tiles), kThreads, kSmem, ctx->stream>>>(ta, tb, static_cast<int>(a.M),
+      static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc, ctx->err_dev);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+
+gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a) {
+  if(a.M == 0 || a.N == 0) return GBPOLY_OK;
+  const bool a_kmaj = a.op_a == GBPOLY_OP_N;
+  const bool b_kmaj = a.op_b == GBPOLY_OP_T;
+  bool tma_ok = aligned16(a.A) && aligned16(a.B) && (a.lda % 4 == 0) && (a.ldb % 4 == 0) && a.K > 0 &&
+                a.M < (1ll << 31) && a.N < (1ll << 31) && a.K < (1ll << 31);
+  if(a.dual) tma_ok = tma_ok && a_kmaj && b_kmaj && a.A2 == a.B && a.B2 == a.A;
+
+  if(!tma_ok) {
+    TiledOperand<float> oa = a_kmaj ? TiledOperand<float>{a.A, a.lda, 1} : TiledOperand<float>{a.A, 1, a.lda};
+    TiledOperand<float> ob = b_kmaj ? TiledOperand<float>{a.B, a.ldb, 1} : TiledOperand<float>{a.B, 1, a.ldb};
+    TiledOperand<float> oa2{a.A2, a.lda2, 1}, ob2{a.B2, a.ldb2, 1};
+    return launch_tiled_gemm<float>(ctx, a.M, a.N, a.K, a.alpha, oa, ob, a.dual, oa2, ob2, a.beta, a.C, a.ldc);
+  }
+
+  CUtensorMap ta, tb;
+  const auto dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  gbpoly_status st;
+  // op(A) is M x K.  Stored as M x K (K-major) for op N, K x M for op T.
+  if(a_kmaj)
+    st = make_tmap_2d(ctx, &ta, dt, 4, a.A, a.M, a.K, a.lda, kBM, kBK, CU_TENSOR_MAP_SWIZZLE_128B);
+  else
+    st = make_tmap_2d(ctx, &ta, dt, 4, a.A, a.K, a.M, a.lda, kBK, kBM, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if(st != GBPOLY_OK) return st;
+  // op(B) is K x N.  Stored as K x N for op N, N x K (K-major) for op T.
+  if(b_kmaj)
+    st = make_tmap_2d(ctx, &tb, dt, 4, a.B, a.N, a.K, a.ldb, kBN, kBK, CU_TENSOR_MAP_SWIZZLE_128B);
+  else
+    st = make_tmap_2d(ctx, &tb, dt, 4, a.B, a.K, a.N, a.ldb, kBK, kBN, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if(st != GBPOLY_OK) return st;
+
+  if(a.dual) return launch_tma<true, true, true, 3>(ctx, a, ta, tb);
+  if(a_kmaj && b_kmaj) return launch_tma<true, true, false, 4>(ctx, a, ta, tb);
+  if(a_kmaj && !b_kmaj) return launch_tma<true, false, false, 4>(ctx, a, ta, tb);
+  if(!a_kmaj && b_kmaj) return launch_tma<false, true, false, 4>(ctx, a, ta, tb);
+  return launch_tma<false, false, false, 4>(ctx, a, ta, tb);
+}
+
+}  // namespace gbpoly

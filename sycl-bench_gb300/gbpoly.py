@@ -1,0 +1,278 @@
+"""ctypes binding of libgbpoly (the C ABI in include/gbpoly.h).
+
+This is the Python face of the same boundary the C++ PolyBench executables
+use.  It loads the in-tree ``lib/libgbpoly.so`` and fails loudly if that
+library has not been built: there is no fallback implementation.
+
+    from gbpoly import Context, Precision
+    with Context(0) as ctx:
+        A = ctx.upload(a_np); B = ctx.upload(b_np); C = ctx.upload(c_np)
+        ctx.gemm(Precision.FP32, M, N, K, 32412.0, A, K, B, N, 2123.0, C, N)
+        out = ctx.download(C, (M, N))
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import enum
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libgbpoly.so"
+
+
+class GbpolyError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"gbpoly status {status}: {message}")
+        self.status = status
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    INVALID = 1
+    CUDA = 2
+    NOMEM = 3
+    TIMEOUT = 4
+    UNSUPPORTED = 5
+    STATE = 6
+
+
+class Precision(enum.IntEnum):
+    FP32 = 0
+    BF16X3 = 1
+    TF32 = 2
+    FP8 = 3
+
+
+class Op(enum.IntEnum):
+    N = 0
+    T = 1
+
+
+_c_i64 = ct.c_int64
+_vp = ct.c_void_p
+
+# name -> (restype, argtypes); every exported symbol of include/gbpoly.h
+SIGNATURES: dict[str, tuple] = {
+    "gbpoly_init": (ct.c_int, [ct.c_int, ct.POINTER(_vp)]),
+    "gbpoly_destroy": (ct.c_int, [_vp]),
+    "gbpoly_last_error": (ct.c_char_p, []),
+    "gbpoly_device_name": (ct.c_int, [_vp, ct.c_char_p, ct.c_size_t]),
+    "gbpoly_device_props": (ct.c_int, [_vp] + [ct.POINTER(ct.c_int)] * 4),
+    "gbpoly_synchronize": (ct.c_int, [_vp]),
+    "gbpoly_set_stream": (ct.c_int, [_vp, _vp]),
+    "gbpoly_malloc": (ct.c_int, [_vp, ct.POINTER(_vp), ct.c_size_t]),
+    "gbpoly_free": (ct.c_int, [_vp, _vp]),
+    "gbpoly_host_alloc": (ct.c_int, [_vp, ct.POINTER(_vp), ct.c_size_t]),
+    "gbpoly_host_free": (ct.c_int, [_vp, _vp]),
+    "gbpoly_memcpy_h2d": (ct.c_int, [_vp, _vp, _vp, ct.c_size_t]),
+    "gbpoly_memcpy_d2h": (ct.c_int, [_vp, _vp, _vp, ct.c_size_t]),
+    "gbpoly_memcpy_d2d": (ct.c_int, [_vp, _vp, _vp, ct.c_size_t]),
+    "gbpoly_memset": (ct.c_int, [_vp, _vp, ct.c_int, ct.c_size_t]),
+    "gbpoly_event_create": (ct.c_int, [_vp, ct.POINTER(_vp)]),
+    "gbpoly_event_destroy": (ct.c_int, [_vp, _vp]),
+    "gbpoly_event_record": (ct.c_int, [_vp, _vp]),
+    "gbpoly_event_elapsed_ms": (ct.c_int, [_vp, _vp, _vp, ct.POINTER(ct.c_float)]),
+    "gbpoly_gemm_f32": (ct.c_int, [_vp, ct.c_int, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
+                                   _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
+    "gbpoly_syrk_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, ct.c_float, _vp,
+                                   _c_i64]),
+    "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
+                                    ct.c_float, _vp, _c_i64]),
+    "gbpoly_gemm_f64": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, _vp,
+                                   _c_i64, ct.c_double, _vp, _c_i64]),
+    "gbpoly_syrk_f64": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, ct.c_double, _vp, _c_i64]),
+    "gbpoly_syr2k_f64": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, _vp, _c_i64, ct.c_double, _vp,
+                                    _c_i64]),
+    "gbpoly_convert_f32_f64": (ct.c_int, [_vp, _vp, _vp, _c_i64]),
+    "gbpoly_error_norms": (ct.c_int, [_vp, _vp, _c_i64, _vp, _c_i64, _c_i64, _c_i64, ct.POINTER(ct.c_double),
+                                      ct.POINTER(ct.c_double), ct.POINTER(ct.c_double)]),
+}
+
+_lib = None
+
+
+def load_library(path: Path | None = None) -> ct.CDLL:
+    """Load libgbpoly.so and bind every signature; raise if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path or os.environ.get("GBPOLY_LIB", LIB_PATH))
+    if not p.exists():
+        raise RuntimeError(f"libgbpoly.so not found at {p}: build it with "
+                           f"`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ct.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        msg = _lib.gbpoly_last_error().decode(errors="replace") if _lib else ""
+        raise GbpolyError(status, msg)
+
+
+class DeviceBuffer:
+    """Owning handle of a device allocation made through gbpoly_malloc."""
+
+    def __init__(self, ctx: "Context", nbytes: int):
+        self.ctx = ctx
+        self.nbytes = nbytes
+        p = _vp()
+        _check(ctx.lib.gbpoly_malloc(ctx.handle, ct.byref(p), nbytes))
+        self.ptr = p.value or 0
+
+    def free(self) -> None:
+        if self.ptr:
+            _check(self.ctx.lib.gbpoly_free(self.ctx.handle, _vp(self.ptr)))
+            self.ptr = 0
+
+    def __int__(self) -> int:
+        return self.ptr
+
+
+class Event:
+    def __init__(self, ctx: "Context"):
+        self.ctx = ctx
+        h = _vp()
+        _check(ctx.lib.gbpoly_event_create(ctx.handle, ct.byref(h)))
+        self.handle = h
+
+    def record(self) -> None:
+        _check(self.ctx.lib.gbpoly_event_record(self.ctx.handle, self.handle))
+
+    def elapsed_ms(self, end: "Event") -> float:
+        ms = ct.c_float()
+        _check(self.ctx.lib.gbpoly_event_elapsed_ms(self.ctx.handle, self.handle, end.handle, ct.byref(ms)))
+        return float(ms.value)
+
+    def destroy(self) -> None:
+        if self.handle:
+            self.ctx.lib.gbpoly_event_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+
+def _ptr(x) -> _vp:
+    if isinstance(x, DeviceBuffer):
+        return _vp(x.ptr)
+    if isinstance(x, np.ndarray):
+        return _vp(x.ctypes.data)
+    return _vp(int(x) if x else None)
+
+
+class Context:
+    """One device, one stream.  Mirrors the reference's BenchmarkArgs::device_queue."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = _vp()
+        _check(self.lib.gbpoly_init(device, ct.byref(h)))
+        self.handle = h
+        self._buffers: list[DeviceBuffer] = []
+
+    # -- lifetime
+    def close(self) -> None:
+        if self.handle:
+            for b in self._buffers:
+                try:
+                    b.free()
+                except GbpolyError:
+                    pass
+            self._buffers.clear()
+            self.lib.gbpoly_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- device info
+    def device_name(self) -> str:
+        buf = ct.create_string_buffer(256)
+        _check(self.lib.gbpoly_device_name(self.handle, buf, 256))
+        return buf.value.decode()
+
+    def device_props(self) -> dict:
+        v = [ct.c_int() for _ in range(4)]
+        _check(self.lib.gbpoly_device_props(self.handle, *[ct.byref(x) for x in v]))
+        return {"sm_count": v[0].value, "sm_clock_khz": v[1].value, "cc": (v[2].value, v[3].value)}
+
+    def synchronize(self) -> None:
+        _check(self.lib.gbpoly_synchronize(self.handle))
+
+    # -- memory
+    def alloc(self, nbytes: int) -> DeviceBuffer:
+        b = DeviceBuffer(self, nbytes)
+        self._buffers.append(b)
+        return b
+
+    def free(self, buf: DeviceBuffer) -> None:
+        buf.free()
+        if buf in self._buffers:
+            self._buffers.remove(buf)
+
+    def upload(self, arr: np.ndarray) -> DeviceBuffer:
+        arr = np.ascontiguousarray(arr)
+        b = self.alloc(arr.nbytes)
+        self.h2d(b, arr)
+        self.synchronize()
+        return b
+
+    def h2d(self, dst, src: np.ndarray, nbytes: int | None = None) -> None:
+        _check(self.lib.gbpoly_memcpy_h2d(self.handle, _ptr(dst), _ptr(src), src.nbytes if nbytes is None else nbytes))
+
+    def d2h(self, dst: np.ndarray, src, nbytes: int | None = None) -> None:
+        _check(self.lib.gbpoly_memcpy_d2h(self.handle, _ptr(dst), _ptr(src), dst.nbytes if nbytes is None else nbytes))
+
+    def download(self, buf, shape, dtype=np.float32) -> np.ndarray:
+        out = np.empty(shape, dtype=dtype)
+        self.d2h(out, buf)
+        self.synchronize()
+        return out
+
+    def memset(self, buf, value: int, nbytes: int) -> None:
+        _check(self.lib.gbpoly_memset(self.handle, _ptr(buf), value, nbytes))
+
+    def event(self) -> Event:
+        return Event(self)
+
+    # -- contractions (asynchronous; call synchronize() to wait and to collect errors)
+    def gemm(self, prec, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, op_a=Op.N, op_b=Op.N) -> None:
+        _check(self.lib.gbpoly_gemm_f32(self.handle, int(prec), int(op_a), int(op_b), M, N, K, alpha, _ptr(A), lda,
+                                        _ptr(B), ldb, beta, _ptr(C), ldc))
+
+    def syrk(self, prec, N, K, alpha, A, lda, beta, C, ldc) -> None:
+        _check(self.lib.gbpoly_syrk_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, beta, _ptr(C), ldc))
+
+    def syr2k(self, prec, N, K, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
+        _check(self.lib.gbpoly_syr2k_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta,
+                                         _ptr(C), ldc))
+
+    # -- FP64
+    def gemm_f64(self, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, op_a=Op.N, op_b=Op.N) -> None:
+        _check(self.lib.gbpoly_gemm_f64(self.handle, int(op_a), int(op_b), M, N, K, alpha, _ptr(A), lda, _ptr(B), ldb,
+                                        beta, _ptr(C), ldc))
+
+    def syrk_f64(self, N, K, alpha, A, lda, beta, C, ldc) -> None:
+        _check(self.lib.gbpoly_syrk_f64(self.handle, N, K, alpha, _ptr(A), lda, beta, _ptr(C), ldc))
+
+    def syr2k_f64(self, N, K, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
+        _check(self.lib.gbpoly_syr2k_f64(self.handle, N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(C), ldc))
+
+    def convert_f32_f64(self, src, dst, count: int) -> None:
+        _check(self.lib.gbpoly_convert_f32_f64(self.handle, _ptr(src), _ptr(dst), count))
+
+    def error_norms(self, C, ldc, R, ldr, rows, cols) -> tuple[float, float, float]:
+        a, b, c = ct.c_double(), ct.c_double(), ct.c_double()
+        _check(self.lib.gbpoly_error_norms(self.handle, _ptr(C), ldc, _ptr(R), ldr, rows, cols, ct.byref(a),
+                                           ct.byref(b), ct.byref(c)))
+        return float(a.value), float(b.value), float(c.value)

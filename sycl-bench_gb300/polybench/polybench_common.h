@@ -1,0 +1,321 @@
+// Shared pieces of the five PolyBench contraction benchmarks.
+//
+//  * percentDiff / absVal: the verification comparator of
+//    polybench/common/polybenchUtilFuncts.h:27-42 (float narrowing kept).
+//  * Benchmark-specific options, read through args.cli like the reference's
+//    own extra options (include/command_line.h:98-103):
+//      --precision=fp32|bf16x3|tf32|fp8[,...]  arithmetic form(s) to run (fp32)
+//      --init=polybench|uniform|normal          input initialisation (polybench)
+//      --seed=<u64>                             seed of uniform/normal inputs (1)
+//      --alpha=<f> --beta=<f>                   override syrk/syr2k/gemm scalars
+//      --verification-oracle=host|fp64          host FP32 loop of the reference
+//                                               (default) or an FP64 reference
+//      --error-report=<file.jsonl>              append max/Frobenius error vs FP64
+//  * Memoised oracles: the reference recomputes its O(N^3) host loop after
+//    every run (include/common.h:113-121); the result depends only on the
+//    benchmark, size and inputs, so it is computed once per process.
+//  * Host-device kernels for --device=cpu: the reference kernel bodies run
+//    on the host cores (OpenMP over output rows, each element keeps its
+//    sequential k order).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "common.h"
+#include "gbpoly.h"
+
+// ------------------------------------------------------------- comparator --
+#define SMALL_FLOAT_VAL 0.00000001f
+
+inline float absVal(float a) { return a < 0 ? a * -1 : a; }
+
+inline float percentDiff(double val1, double val2) {
+  if(absVal(val1) < 0.01 && absVal(val2) < 0.01) return 0.0f;
+  return 100.0f * absVal(absVal(val1 - val2) / absVal(val1 + SMALL_FLOAT_VAL));
+}
+
+namespace poly {
+
+constexpr double kErrorThreshold = 0.05;  // percent (gemm.cpp:96 and the other four)
+
+// ---------------------------------------------------------------- options --
+enum class Init { Polybench, Uniform, Normal };
+
+struct Options {
+  gbpoly_precision precision = GBPOLY_PREC_FP32;
+  Init init = Init::Polybench;
+  uint64_t seed = 1;
+  bool fp64_oracle = false;
+  std::string error_report;
+  bool has_alpha = false, has_beta = false;
+  double alpha = 0, beta = 0;
+};
+
+inline const char* precision_name(gbpoly_precision p) {
+  switch(p) {
+  case GBPOLY_PREC_FP32: return "fp32";
+  case GBPOLY_PREC_BF16X3: return "bf16x3";
+  case GBPOLY_PREC_TF32: return "tf32";
+  case GBPOLY_PREC_FP8: return "fp8";
+  }
+  return "?";
+}
+
+inline gbpoly_precision parse_precision(const std::string& s) {
+  if(s == "fp32") return GBPOLY_PREC_FP32;
+  if(s == "bf16x3") return GBPOLY_PREC_BF16X3;
+  if(s == "tf32") return GBPOLY_PREC_TF32;
+  if(s == "fp8") return GBPOLY_PREC_FP8;
+  throw std::invalid_argument{"unknown --precision value: " + s};
+}
+
+inline std::vector<gbpoly_precision> precisions(const BenchmarkArgs& args) {
+  std::vector<gbpoly_precision> out;
+  std::stringstream in(args.cli.getOrDefault<std::string>("--precision", "fp32"));
+  std::string item;
+  while(std::getline(in, item, ',')) out.push_back(parse_precision(item));
+  return out;
+}
+
+inline Options options(const BenchmarkArgs& args, gbpoly_precision prec) {
+  Options o;
+  o.precision = prec;
+  const std::string init = args.cli.getOrDefault<std::string>("--init", "polybench");
+  if(init == "polybench")
+    o.init = Init::Polybench;
+  else if(init == "uniform")
+    o.init = Init::Uniform;
+  else if(init == "normal")
+    o.init = Init::Normal;
+  else
+    throw std::invalid_argument{"unknown --init value: " + init};
+  o.seed = args.cli.getOrDefault<uint64_t>("--seed", 1);
+  const std::string orc = args.cli.getOrDefault<std::string>("--verification-oracle", "host");
+  if(orc != "host" && orc != "fp64") throw std::invalid_argument{"unknown --verification-oracle value: " + orc};
+  o.fp64_oracle = orc == "fp64";
+  o.error_report = args.cli.getOrDefault<std::string>("--error-report", "");
+  o.has_alpha = args.cli.isArgSet("--alpha");
+  o.has_beta = args.cli.isArgSet("--beta");
+  if(o.has_alpha) o.alpha = args.cli.get<double>("--alpha");
+  if(o.has_beta) o.beta = args.cli.get<double>("--beta");
+  return o;
+}
+
+// Benchmark name: the reference's name for the default configuration, with
+// suffixes for every non-default choice (element type, form, inputs, scalars).
+template <class T>
+std::string variant_name(const std::string& base, const Options& o) {
+  std::string n = base;
+  if(std::is_same<T, double>::value) n += std::string("_") + ReadableTypename<double>::name;
+  if(o.precision != GBPOLY_PREC_FP32) n += std::string("_") + precision_name(o.precision);
+  if(o.init == Init::Uniform) n += "_uniform_seed" + std::to_string(o.seed);
+  if(o.init == Init::Normal) n += "_normal_seed" + std::to_string(o.seed);
+  if(o.has_alpha || o.has_beta) {
+    std::ostringstream s;
+    s << "_ab" << (o.has_alpha ? o.alpha : 0) << "_" << (o.has_beta ? o.beta : 0);
+    n += s.str();
+  }
+  return n;
+}
+
+// ------------------------------------------------------- seeded variants --
+// splitmix64: a fixed, platform-independent stream.
+struct Rng {
+  uint64_t s;
+  explicit Rng(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  double uniform01() { return double(next() >> 11) * (1.0 / 9007199254740992.0); }  // [0, 1)
+};
+
+// Fill `count` values uniform in [-1, 1) or standard normal (Box-Muller),
+// stream `which` of the seed (one stream per matrix).
+template <class T>
+void fill_random(T* p, std::size_t count, Init kind, uint64_t seed, uint64_t which) {
+  Rng r(seed * 0x100000001B3ull + which * 0xC2B2AE3D27D4EB4Full + 7);
+  if(kind == Init::Uniform) {
+    for(std::size_t i = 0; i < count; ++i) p[i] = static_cast<T>(2.0 * r.uniform01() - 1.0);
+  } else {
+    for(std::size_t i = 0; i < count; i += 2) {
+      const double u1 = 1.0 - r.uniform01(), u2 = r.uniform01();
+      const double rad = std::sqrt(-2.0 * std::log(u1)), th = 6.283185307179586 * u2;
+      p[i] = static_cast<T>(rad * std::cos(th));
+      if(i + 1 < count) p[i + 1] = static_cast<T>(rad * std::sin(th));
+    }
+  }
+}
+
+// ------------------------------------------------------------ memoisation --
+template <class T>
+std::shared_ptr<const std::vector<T>> memo(const std::string& key, const std::function<std::vector<T>()>& make) {
+  static std::map<std::string, std::shared_ptr<const std::vector<T>>> cache;
+  auto it = cache.find(key);
+  if(it != cache.end()) return it->second;
+  auto v = std::make_shared<const std::vector<T>>(make());
+  cache[key] = v;
+  return v;
+}
+
+inline std::string memo_key(const std::string& name, std::size_t n, const Options& o, const char* kind) {
+  return name + "|" + std::to_string(n) + "|" + std::to_string(int(o.init)) + "|" + std::to_string(o.seed) + "|" +
+         std::to_string(o.alpha) + "|" + std::to_string(o.beta) + "|" + kind;
+}
+
+// ----------------------------------------------------------- verification --
+// Row-major walk, first element over the threshold fails (gemm.cpp:107-113).
+template <class T, class R>
+bool compare(const R* reference, const T* device, std::size_t count) {
+  for(std::size_t i = 0; i < count; ++i)
+    if(percentDiff(reference[i], device[i]) > kErrorThreshold) return false;
+  return true;
+}
+
+struct ErrorNorms {
+  double max_rel = 0, frob_rel = 0, max_elem_rel = 0;
+};
+
+template <class T>
+ErrorNorms error_norms(const T* c, const double* r, std::size_t count) {
+  double me = 0, mr = 0, se = 0, sr = 0, mer = 0;
+  bool bad = false;
+  for(std::size_t i = 0; i < count; ++i) {
+    const double e = std::fabs(double(c[i]) - r[i]), a = std::fabs(r[i]);
+    if(!std::isfinite(e)) bad = true;
+    me = std::max(me, e);
+    mr = std::max(mr, a);
+    se += e * e;
+    sr += a * a;
+    if(a > 0) mer = std::max(mer, e / a);
+  }
+  ErrorNorms n;
+  if(bad) {
+    n.max_rel = n.frob_rel = n.max_elem_rel = HUGE_VAL;
+    return n;
+  }
+  n.max_rel = mr > 0 ? me / mr : me;
+  n.frob_rel = sr > 0 ? std::sqrt(se / sr) : std::sqrt(se);
+  n.max_elem_rel = mer;
+  return n;
+}
+
+inline void append_error_report(const Options& o, const std::string& bench, std::size_t n, const std::string& device,
+    const ErrorNorms& e, bool passed) {
+  if(o.error_report.empty()) return;
+  std::ofstream f(o.error_report, std::ios::app);
+  char buf[768];
+  snprintf(buf, sizeof buf,
+      "{\"benchmark\": \"%s\", \"size\": %zu, \"precision\": \"%s\", \"init\": \"%s\", \"seed\": %llu, "
+      "\"device\": \"%s\", \"max_rel\": %.6e, \"frob_rel\": %.6e, \"max_elem_rel\": %.6e, \"verification\": \"%s\"}",
+      bench.c_str(), n, precision_name(o.precision),
+      o.init == Init::Polybench ? "polybench" : (o.init == Init::Uniform ? "uniform" : "normal"),
+      (unsigned long long)o.seed, device.c_str(), e.max_rel, e.frob_rel, e.max_elem_rel, passed ? "PASS" : "FAIL");
+  f << buf << "\n";
+}
+
+// ---------------------------------------------------- FP64 reference steps --
+// A device-side FP64 contraction sequence over N x N matrices, used for the
+// FP64 oracle on the GPU: upload FP32 inputs as FP64, run DGEMMs, read back.
+class Fp64Device {
+public:
+  Fp64Device(const gb::Queue& q, std::size_t n) : q_(q), n_(n) {}
+  ~Fp64Device() {
+    for(void* p : owned_) gbpoly_free(q_.ctx(), p);
+  }
+  template <class T>
+  double* upload(const T* host) {
+    double* d = alloc();
+    if(std::is_same<T, double>::value) {
+      gb::check(gbpoly_memcpy_h2d(q_.ctx(), d, host, bytes()), "h2d");
+    } else {
+      float* tmp = nullptr;
+      gb::check(gbpoly_malloc(q_.ctx(), reinterpret_cast<void**>(&tmp), n_ * n_ * sizeof(float)), "malloc");
+      owned_.push_back(tmp);
+      gb::check(gbpoly_memcpy_h2d(q_.ctx(), tmp, host, n_ * n_ * sizeof(float)), "h2d");
+      gb::check(gbpoly_convert_f32_f64(q_.ctx(), tmp, d, int64_t(n_ * n_)), "convert");
+    }
+    return d;
+  }
+  double* zeros() {
+    double* d = alloc();
+    gb::check(gbpoly_memset(q_.ctx(), d, 0, bytes()), "memset");
+    return d;
+  }
+  // C = alpha * op(A) op(B) + beta * C
+  void gemm(gbpoly_op oa, gbpoly_op ob, double alpha, const double* A, const double* B, double beta, double* C) {
+    const int64_t n = int64_t(n_);
+    gb::check(gbpoly_gemm_f64(q_.ctx(), oa, ob, n, n, n, alpha, A, n, B, n, beta, C, n), "dgemm");
+  }
+  std::vector<double> download(const double* d) {
+    std::vector<double> h(n_ * n_);
+    gb::check(gbpoly_memcpy_d2h(q_.ctx(), h.data(), d, bytes()), "d2h");
+    q_.wait_and_throw();
+    return h;
+  }
+
+private:
+  std::size_t bytes() const { return n_ * n_ * sizeof(double); }
+  double* alloc() {
+    double* d = nullptr;
+    gb::check(gbpoly_malloc(q_.ctx(), reinterpret_cast<void**>(&d), bytes()), "malloc");
+    owned_.push_back(d);
+    return d;
+  }
+  gb::Queue q_;
+  std::size_t n_;
+  std::vector<void*> owned_;
+};
+
+// Host FP64 contraction C = alpha * op(A) op(B) + beta * C (N x N), OpenMP over rows.
+template <class TA>
+void host_gemm_f64(std::size_t n, bool ta, bool tb, double alpha, const TA* A, const TA* B, double beta,
+    std::vector<double>& C) {
+#pragma omp parallel for schedule(static)
+  for(long i = 0; i < long(n); ++i)
+    for(std::size_t j = 0; j < n; ++j) {
+      double s = 0;
+      for(std::size_t k = 0; k < n; ++k)
+        s += double(ta ? A[k * n + i] : A[i * n + k]) * double(tb ? B[j * n + k] : B[k * n + j]);
+      C[i * n + j] = alpha * s + beta * C[i * n + j];
+    }
+}
+
+// ------------------------------------------------- host-device kernel bodies --
+// C[i][j] = beta*C[i][j] + sum_k (alpha*op(A)[i][k]) * op(B)[k][j], each element
+// walking k in order; OpenMP over rows, 64-wide column blocks vectorised.
+template <class T>
+void host_gemm_body(std::size_t n, bool tb, T alpha, const T* A, const T* B, T beta, T* C) {
+  constexpr std::size_t V = 64;
+#pragma omp parallel for schedule(static)
+  for(long i = 0; i < long(n); ++i) {
+    for(std::size_t j0 = 0; j0 < n; j0 += V) {
+      const std::size_t j1 = std::min(n, j0 + V);
+      T acc[V];
+      for(std::size_t j = j0; j < j1; ++j) acc[j - j0] = C[i * n + j] * beta;
+      for(std::size_t k = 0; k < n; ++k) {
+        const T a = alpha * A[i * n + k];
+        if(tb)
+          for(std::size_t j = j0; j < j1; ++j) acc[j - j0] += a * B[j * n + k];
+        else
+          for(std::size_t j = j0; j < j1; ++j) acc[j - j0] += a * B[k * n + j];
+      }
+      for(std::size_t j = j0; j < j1; ++j) C[i * n + j] = acc[j - j0];
+    }
+  }
+}
+
+}  // namespace poly
