@@ -33,6 +33,9 @@ import numpy as np  # noqa: E402
 ALPHA, BETA = 32412.0, 2123.0
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of the same kernel and workload (profiles/ holds the summaries).
+TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {}
 
 
 # ------------------------------------------------------------------ helpers
@@ -178,8 +181,8 @@ def run_gpu(args, dist: Dist) -> dict | None:
     def fresh_c():
         ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(dC), gbpoly._ptr(dC0), nbytes)
 
-    forms = [Precision.FP32]
-    headline = Precision.FP32
+    forms = [Precision.FP32, Precision.BF16X3]
+    headline = Precision.BF16X3
     tiers = {}
     sampler = ClockSampler(dist.local_rank)
     sampler.start()
@@ -195,6 +198,8 @@ def run_gpu(args, dist: Dist) -> dict | None:
         ev0, ev1 = ctx.event(), ctx.event()
         dist.barrier()
         ctx.synchronize()
+        ctx.profile_read()  # drop records of earlier launches
+        ctx.profile(True)
         t0 = time.time()
         ev0.record()
         for _ in range(args.steps):
@@ -202,15 +207,21 @@ def run_gpu(args, dist: Dist) -> dict | None:
         ev1.record()
         ctx.synchronize()
         t1 = time.time()
+        ctx.profile(False)
+        kernels = ctx.profile_read()
         dist.barrier()
         ms = ev0.elapsed_ms(ev1) / args.steps
         ms = dist.max(ms)
         if prec == headline:
             timed_window = (t0, t1)
+        top = max(kernels.items(), key=lambda kv: kv[1][1])
         tiers[prec.name.lower()] = {
             "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12 * dist.world,
             "err_vs_fp64": {"max_rel": max_rel, "frob_rel": frob, "max_elem_rel": elem},
-            "kernel_launches_per_step": 1,
+            "kernel_launches_per_step": sum(c for c, _ in kernels.values()) / args.steps,
+            "kernels": {k: {"launches": c, "avg_ms": t / c, "share": t / sum(x[1] for x in kernels.values())}
+                        for k, (c, t) in kernels.items()},
+            "dominant_kernel": top[0], "dominant_avg_ms": top[1][1] / top[1][0],
         }
         ev0.destroy()
         ev1.destroy()
@@ -251,20 +262,30 @@ def run_gpu(args, dist: Dist) -> dict | None:
 
     head = tiers[headline.name.lower()]
     peaks, peak_kind = load_peaks()
+    kernel_tflops = flops / (head["dominant_avg_ms"] * 1e-3) / 1e12
     if headline == Precision.FP32:
         # FFMA pipe: SMs x 128 lanes x 2 FLOP x max SM clock (no measured FP32 figure exists)
         clk_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz") or props["sm_clock_khz"] / 1e3
         peak = props["sm_count"] * 128 * 2 * clk_mhz * 1e6 / 1e12
-        roof = {"bound": "fp32_simt", "achieved": head["tflops"] / dist.world, "peak": peak, "unit": "TFLOP/s",
-                "frac": head["tflops"] / dist.world / peak, "traffic": None,
+        roof = {"bound": "fp32_simt", "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": kernel_tflops / peak, "traffic": None,
                 "peak_source": f"computed: {props['sm_count']} SMs x 128 FFMA lanes x 2 x {clk_mhz:.0f} MHz"}
+    else:
+        # split-BF16 runs 3 BF16 MMAs per algorithmic multiply-add: its ceiling is the BF16 peak / 3
+        bf16 = peaks["bf16_tflops"]
+        peak = bf16 / 3.0
+        roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": kernel_tflops / peak, "traffic": TRAFFIC_PER_LAUNCH.get((head["dominant_kernel"], n)),
+                "kernel": head["dominant_kernel"], "kernel_avg_ms": head["dominant_avg_ms"],
+                "peak_source": f"{bf16} TFLOP/s dense BF16 burst ({peak_kind}) / 3 MMAs per multiply-add",
+                "frac_of_bf16_peak_tensor_work": 3 * kernel_tflops / bf16}
     ctx.close()
     return {
         "value": head["tflops"], "ms_per_step": head["ms_per_step"], "tiers": tiers, "clocks": clocks,
         "roofline": roof, "headline": headline.name.lower(),
         "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 * dist.world, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
-        "gpu_launches": args.steps * head["kernel_launches_per_step"],
+        "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
         "device": props, "peak_kind": peak_kind,
     }
 
@@ -343,7 +364,7 @@ def main() -> None:
                          f"cores ({r['seconds']:.1f} s), oracle port built -O3 -march=native -ffast-math"}
     if dist.rank == 0:
         line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"],
-                    dtype="f32" if res["headline"] == "fp32" else "bf16x3 (fp32 in/out)",
+                    dtype="f32" if res["headline"] == "fp32" else "bf16x3 (f32 in/out, bf16 hi/lo products, f32 accumulate)",
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},

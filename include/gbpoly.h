@@ -42,7 +42,9 @@ typedef enum {
   GBPOLY_PREC_FP32 = 0,   /* plain FP32 SIMT FFMA kernels: the drop-in form */
   GBPOLY_PREC_BF16X3 = 1, /* split-BF16: hi*hi + hi*lo + lo*hi on tcgen05, FP32 accumulation in TMEM */
   GBPOLY_PREC_TF32 = 2,   /* tcgen05 kind::tf32, FP32 accumulation */
-  GBPOLY_PREC_FP8 = 3     /* e4m3 with one scale per 128x128 operand tile */
+  GBPOLY_PREC_FP8 = 3,    /* e4m3 with one scale per 128x128 operand tile */
+  GBPOLY_PREC_TF32X3 = 4, /* split-TF32: hi*hi + hi*lo + lo*hi on kind::tf32 (hi+lo keep ~24 bits: FP32-level error) */
+  GBPOLY_PREC_BF16X6 = 5  /* three-way split-BF16: the 6 products of order <= 2^-16 (FP32-level error) */
 } gbpoly_precision;
 
 /* Operand transposition: OP_N uses the matrix as stored, OP_T its transpose. */
@@ -108,6 +110,18 @@ gbpoly_status gbpoly_event_destroy(gbpoly_ctx* ctx, gbpoly_event* ev);
 gbpoly_status gbpoly_event_record(gbpoly_ctx* ctx, gbpoly_event* ev);
 /* Milliseconds between two recorded events (waits for `end`). */
 gbpoly_status gbpoly_event_elapsed_ms(gbpoly_ctx* ctx, gbpoly_event* start, gbpoly_event* end, float* ms);
+
+/* Per-kernel timing.  While enabled, every kernel the library launches on the
+ * context's stream is bracketed by CUDA events, so a caller can separate the
+ * kernels one contraction call launches (the per-kernel view of the
+ * reference's kernel-time, include/common.h:86-99). */
+gbpoly_status gbpoly_profile_enable(gbpoly_ctx* ctx, int enable);
+/* Waits for the stream, then aggregates the launches recorded since the last
+ * read by kernel: names (64 bytes each), launch counts, total milliseconds.
+ * *n_entries receives the number of distinct kernels (entries beyond
+ * max_entries are dropped).  Clears the record. */
+gbpoly_status gbpoly_profile_read(gbpoly_ctx* ctx, int max_entries, char* names, int* counts, double* total_ms,
+    int* n_entries);
 
 /* ----------------------------------------------------------- contractions -- */
 

@@ -34,7 +34,13 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"] + ARCH
-CXX_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-Wall", "-Wno-unknown-pragmas"]
+# The benchmarks' host oracle loops compare against the reference's own FP32
+# loops: no -ffast-math and no FMA contraction, so the host results are the
+# reference's operation order on every host ISA.  Double variants and queue
+# profiling are on (sycl-bench's SYCL_BENCH_HAS_FP64_SUPPORT /
+# SYCL_BENCH_ENABLE_QUEUE_PROFILING).
+CXX_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
+             "-DSYCL_BENCH_HAS_FP64_SUPPORT=1", "-DSYCL_BENCH_ENABLE_QUEUE_PROFILING=1"]
 
 BENCHMARKS = ["gemm", "2mm", "3mm", "syrk", "syr2k"]
 

@@ -43,6 +43,32 @@ gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) {
   return GBPOLY_OK;
 }
 
+namespace {
+cudaEvent_t pooled_event(gbpoly_ctx* ctx) {
+  if(!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if(cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+}  // namespace
+
+ProfileScope::ProfileScope(gbpoly_ctx* ctx, const char* kernel) : ctx_(ctx) {
+  if(!ctx->profiling) return;
+  ProfileRecord r{kernel, pooled_event(ctx), pooled_event(ctx)};
+  if(!r.start || !r.end) return;
+  cudaEventRecord(r.start, ctx->stream);
+  index_ = ctx->prof.size();
+  ctx->prof.push_back(r);
+}
+
+ProfileScope::~ProfileScope() {
+  if(index_ != size_t(-1)) cudaEventRecord(ctx_->prof[index_].end, ctx_->stream);
+}
+
 gbpoly_status make_tmap_2d(gbpoly_ctx* ctx, CUtensorMap* map, CUtensorMapDataType dtype, size_t elem_bytes,
     const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols,
     CUtensorMapSwizzle swizzle) {
@@ -148,6 +174,11 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if(ctx->ws.ptr) cudaFree(ctx->ws.ptr);
+  for(auto& r : ctx->prof) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.end);
+  }
+  for(auto e : ctx->event_pool) cudaEventDestroy(e);
   if(ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if(ctx->err_host) cudaFreeHost(ctx->err_host);
   delete ctx;
@@ -186,6 +217,47 @@ gbpoly_status gbpoly_synchronize(gbpoly_ctx* ctx) {
 gbpoly_status gbpoly_set_stream(gbpoly_ctx* ctx, void* cuda_stream) {
   if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
   ctx->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : ctx->own_stream;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_profile_enable(gbpoly_ctx* ctx, int enable) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  ctx->profiling = enable != 0;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_profile_read(gbpoly_ctx* ctx, int max_entries, char* names, int* counts, double* total_ms,
+    int* n_entries) {
+  CTX_TRY(ctx);
+  if(max_entries < 0 || (max_entries > 0 && (!names || !counts || !total_ms)) || !n_entries)
+    return fail(GBPOLY_ERR_INVALID, "bad argument");
+  GBPOLY_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  std::vector<std::string> keys;
+  std::vector<int> cnt;
+  std::vector<double> tot;
+  for(auto& r : ctx->prof) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.start, r.end);
+    size_t i = 0;
+    while(i < keys.size() && keys[i] != r.kernel) ++i;
+    if(i == keys.size()) {
+      keys.push_back(r.kernel);
+      cnt.push_back(0);
+      tot.push_back(0.0);
+    }
+    cnt[i] += 1;
+    tot[i] += ms;
+    ctx->event_pool.push_back(r.start);
+    ctx->event_pool.push_back(r.end);
+  }
+  ctx->prof.clear();
+  *n_entries = int(keys.size());
+  for(int i = 0; i < int(keys.size()) && i < max_entries; ++i) {
+    strncpy(names + 64 * i, keys[i].c_str(), 63);
+    names[64 * i + 63] = 0;
+    counts[i] = cnt[i];
+    total_ms[i] = tot[i];
+  }
   return GBPOLY_OK;
 }
 
@@ -298,6 +370,10 @@ gbpoly_status gbpoly_gemm_f32(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op 
   a.A = A, a.lda = lda, a.B = B, a.ldb = ldb, a.C = C, a.ldc = ldc;
   switch(prec) {
   case GBPOLY_PREC_FP32: return launch_gemm_f32_simt(ctx, a);
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_TF32:
+  case GBPOLY_PREC_TF32X3:
+  case GBPOLY_PREC_BF16X6: return launch_gemm_tensor(ctx, prec, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
   }
 }
@@ -321,6 +397,10 @@ gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N
   a.dual = true, a.A2 = B, a.lda2 = ldb, a.B2 = A, a.ldb2 = lda;
   switch(prec) {
   case GBPOLY_PREC_FP32: return launch_gemm_f32_simt(ctx, a);
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_TF32:
+  case GBPOLY_PREC_TF32X3:
+  case GBPOLY_PREC_BF16X6: return launch_gemm_tensor(ctx, prec, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
   }
 }

@@ -143,6 +143,7 @@ gbpoly_status gbpoly_convert_f32_f64(gbpoly_ctx* ctx, const float* src, double* 
   if(count == 0) return GBPOLY_OK;
   if(!src || !dst) return fail(GBPOLY_ERR_INVALID, "null pointer");
   const int64_t blocks = std::min<int64_t>((count + 255) / 256, int64_t(ctx->sm_count) * 16);
+  ProfileScope prof(ctx, "convert_f32_f64");
   convert_f32_f64_kernel<<<static_cast<unsigned>(blocks), 256, 0, ctx->stream>>>(src, dst, count);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
@@ -161,6 +162,7 @@ gbpoly_status gbpoly_error_norms(gbpoly_ctx* ctx, const float* C, int64_t ldc, c
     if((st = ensure_workspace(ctx, size_t(blocks + 1) * kStats * sizeof(double))) != GBPOLY_OK) return st;
     double* partial = static_cast<double*>(ctx->ws.ptr);
     double* out = partial + size_t(blocks) * kStats;
+    ProfileScope prof(ctx, "error_norms");
     error_norms_partial_kernel<<<blocks, kNormThreads, 0, ctx->stream>>>(C, ldc, R, ldr, rows, cols, partial);
     GBPOLY_CUDA_TRY(cudaGetLastError());
     error_norms_final_kernel<<<1, kNormThreads, 0, ctx->stream>>>(partial, blocks, out);

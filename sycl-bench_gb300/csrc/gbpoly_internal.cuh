@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/gbpoly.h"
 
@@ -37,6 +38,14 @@ struct Workspace {
 
 }  // namespace gbpoly
 
+namespace gbpoly {
+// One launch bracketed by events while profiling is enabled.
+struct ProfileRecord {
+  const char* kernel;
+  cudaEvent_t start, end;
+};
+}  // namespace gbpoly
+
 struct gbpoly_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -49,6 +58,9 @@ struct gbpoly_ctx {
   char name[256] = {0};
   gbpoly::Workspace ws;
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
+  bool profiling = false;
+  std::vector<gbpoly::ProfileRecord> prof;        // launches since the last read
+  std::vector<cudaEvent_t> event_pool;            // reusable events
 };
 
 namespace gbpoly {
@@ -63,6 +75,18 @@ gbpoly_status cuda_fail(cudaError_t e, const char* what);
     cudaError_t _e = (expr);                                   \
     if(_e != cudaSuccess) return ::gbpoly::cuda_fail(_e, #expr); \
   } while(0)
+
+// Brackets one kernel launch with events when the context is profiling
+// (gbpoly_profile_enable); a no-op otherwise.
+class ProfileScope {
+public:
+  ProfileScope(gbpoly_ctx* ctx, const char* kernel);
+  ~ProfileScope();
+
+private:
+  gbpoly_ctx* ctx_;
+  size_t index_ = size_t(-1);
+};
 
 // Grow the context workspace to at least `bytes` (synchronises when it grows).
 gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes);
@@ -92,6 +116,9 @@ struct GemmF32Args {
   int64_t ldb2 = 0;
 };
 gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
+// Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
+// term panels live in the context workspace.
+gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a);
 
 // ---------------------------------------------------------------- device side
 

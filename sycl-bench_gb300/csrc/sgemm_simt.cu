@@ -262,6 +262,7 @@ gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMa
     attr_set |= 1u << ctx->device;
   }
   const int64_t tiles = ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN);
+  ProfileScope prof(ctx, DUAL ? "sgemm_simt_dual" : "sgemm_simt");
   kern<<<static_cast<unsigned>(tiles), kThreads, kSmem, ctx->stream>>>(ta, tb, static_cast<int>(a.M),
       static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc, ctx->err_dev);
   GBPOLY_CUDA_TRY(cudaGetLastError());

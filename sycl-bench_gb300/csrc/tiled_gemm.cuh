@@ -83,6 +83,7 @@ gbpoly_status launch_tiled_gemm(gbpoly_ctx* ctx, int64_t M, int64_t N, int64_t K
   const int64_t gx = (N + 63) / 64, gy = (M + 63) / 64;
   if(gy > 65535) return fail(GBPOLY_ERR_UNSUPPORTED, "matrix too tall for the tiled kernel grid");
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
+  ProfileScope prof(ctx, sizeof(T) == 8 ? "dgemm_tiled" : "sgemm_tiled");
   tiled_gemm_kernel<T><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, a, b, dual, a2, b2, beta, C, ldc);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;

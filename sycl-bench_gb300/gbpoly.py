@@ -44,6 +44,8 @@ class Precision(enum.IntEnum):
     BF16X3 = 1
     TF32 = 2
     FP8 = 3
+    TF32X3 = 4
+    BF16X6 = 5
 
 
 class Op(enum.IntEnum):
@@ -75,6 +77,9 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_event_destroy": (ct.c_int, [_vp, _vp]),
     "gbpoly_event_record": (ct.c_int, [_vp, _vp]),
     "gbpoly_event_elapsed_ms": (ct.c_int, [_vp, _vp, _vp, ct.POINTER(ct.c_float)]),
+    "gbpoly_profile_enable": (ct.c_int, [_vp, ct.c_int]),
+    "gbpoly_profile_read": (ct.c_int, [_vp, ct.c_int, ct.c_char_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double),
+                                       ct.POINTER(ct.c_int)]),
     "gbpoly_gemm_f32": (ct.c_int, [_vp, ct.c_int, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
                                    _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_syrk_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, ct.c_float, _vp,
@@ -241,6 +246,23 @@ class Context:
 
     def memset(self, buf, value: int, nbytes: int) -> None:
         _check(self.lib.gbpoly_memset(self.handle, _ptr(buf), value, nbytes))
+
+    def profile(self, enable: bool) -> None:
+        _check(self.lib.gbpoly_profile_enable(self.handle, 1 if enable else 0))
+
+    def profile_read(self) -> dict[str, tuple[int, float]]:
+        """{kernel: (launches, total ms)} since the last read."""
+        cap = 32
+        names = ct.create_string_buffer(64 * cap)
+        counts = (ct.c_int * cap)()
+        tot = (ct.c_double * cap)()
+        n = ct.c_int()
+        _check(self.lib.gbpoly_profile_read(self.handle, cap, names, counts, tot, ct.byref(n)))
+        out = {}
+        for i in range(min(n.value, cap)):
+            nm = names.raw[64 * i:64 * i + 64].split(b"\0", 1)[0].decode()
+            out[nm] = (counts[i], tot[i])
+        return out
 
     def event(self) -> Event:
         return Event(self)

@@ -4,7 +4,7 @@
 //    polybench/common/polybenchUtilFuncts.h:27-42 (float narrowing kept).
 //  * Benchmark-specific options, read through args.cli like the reference's
 //    own extra options (include/command_line.h:98-103):
-//      --precision=fp32|bf16x3|tf32|fp8[,...]  arithmetic form(s) to run (fp32)
+//      --precision=fp32|bf16x3|tf32|tf32x3|bf16x6|fp8[,...]  form(s) to run (fp32)
 //      --init=polybench|uniform|normal          input initialisation (polybench)
 //      --seed=<u64>                             seed of uniform/normal inputs (1)
 //      --alpha=<f> --beta=<f>                   override syrk/syr2k/gemm scalars
@@ -68,6 +68,8 @@ inline const char* precision_name(gbpoly_precision p) {
   case GBPOLY_PREC_BF16X3: return "bf16x3";
   case GBPOLY_PREC_TF32: return "tf32";
   case GBPOLY_PREC_FP8: return "fp8";
+  case GBPOLY_PREC_TF32X3: return "tf32x3";
+  case GBPOLY_PREC_BF16X6: return "bf16x6";
   }
   return "?";
 }
@@ -77,6 +79,8 @@ inline gbpoly_precision parse_precision(const std::string& s) {
   if(s == "bf16x3") return GBPOLY_PREC_BF16X3;
   if(s == "tf32") return GBPOLY_PREC_TF32;
   if(s == "fp8") return GBPOLY_PREC_FP8;
+  if(s == "tf32x3") return GBPOLY_PREC_TF32X3;
+  if(s == "bf16x6") return GBPOLY_PREC_BF16X6;
   throw std::invalid_argument{"unknown --precision value: " + s};
 }
 

@@ -1,0 +1,153 @@
+"""Parity of the tensor-core forms (tf32, bf16x3, tf32x3, bf16x6) against the
+oracle, through the C ABI.
+
+Tolerances: the reference's verify rule (every element within 0.05 percent
+of its FP32 host loop, polybench/gemm.cpp:96-113) on the polybench inputs,
+and a normwise Frobenius error against the FP64 oracle on random inputs of
+  tf32    1e-3   (operands rounded to 11 significand bits)
+  bf16x3  2e-5   (hi+lo BF16 keep ~16 bits: ~2^-17 per operand)
+  tf32x3, bf16x6: the FP32 bound 2e-6*sqrt(K) (the terms keep ~24 bits)
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gbpoly import Op, Precision
+
+pytestmark = pytest.mark.gpu
+
+P = Precision.BF16X3
+FORMS = [Precision.TF32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
+VERIFYING = [Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
+
+
+def frob_bound(prec, K):
+    if prec == Precision.TF32:
+        return 1e-3
+    if prec == Precision.BF16X3:
+        return 2e-5
+    return 2e-6 * max(1.0, np.sqrt(K))
+
+
+def run_gemm(ctx, A, B, C, alpha, beta, op_a=Op.N, op_b=Op.N, prec=P):
+    M = A.shape[1] if op_a == Op.T else A.shape[0]
+    K = A.shape[0] if op_a == Op.T else A.shape[1]
+    N = B.shape[0] if op_b == Op.T else B.shape[1]
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.gemm(prec, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, dC, C.shape[1], op_a=op_a, op_b=op_b)
+    ctx.synchronize()
+    out = ctx.download(dC, C.shape)
+    for b in (dA, dB, dC):
+        ctx.free(b)
+    return out
+
+
+def assert_verify(host, dev):
+    first, max_pd, nfail = oracle.verify(host, dev)
+    assert first == -1, f"{nfail} elements over 0.05%, first at {first}, max percentDiff {max_pd}"
+
+
+@pytest.mark.parametrize("prec", VERIFYING)
+@pytest.mark.parametrize("n", [64, 128, 200, 256, 384, 1024])
+def test_gemm_polybench_init_passes_reference_verify(ctx, prec, n):
+    A, B, C = oracle.init_gemm(n)
+    dev = run_gemm(ctx, A, B, C, 32412.0, 2123.0, prec=prec)
+    assert_verify(oracle.host_gemm(n), dev)
+    ref = oracle.gemm_f64(A, B, C, 32412.0, 2123.0)
+    max_rel, frob, _ = oracle.error_norms(dev, ref)
+    assert frob < frob_bound(prec, n), (max_rel, frob)
+
+
+@pytest.mark.parametrize("prec", FORMS)
+@pytest.mark.parametrize("op_a", [Op.N, Op.T])
+@pytest.mark.parametrize("op_b", [Op.N, Op.T])
+@pytest.mark.parametrize("mnk", [(128, 256, 64), (200, 300, 100), (256, 512, 1024), (33, 65, 17), (129, 1, 40)])
+def test_gemm_random_ops_vs_fp64(ctx, prec, op_a, op_b, mnk):
+    M, N, K = mnk
+    rng = np.random.default_rng(M * 7 + N * 3 + K + 11 * int(op_a) + 13 * int(op_b))
+    A = rng.uniform(-1, 1, (K, M) if op_a == Op.T else (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (N, K) if op_b == Op.T else (K, N)).astype(np.float32)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    dev = run_gemm(ctx, A, B, C, 1.5, -0.5, op_a=op_a, op_b=op_b, prec=prec)
+    ref = oracle.gemm_f64(A, B, C, 1.5, -0.5, op_a=int(op_a), op_b=int(op_b))
+    max_rel, frob, _ = oracle.error_norms(dev, ref)
+    assert frob < frob_bound(prec, K), (max_rel, frob)
+
+
+def test_error_relative_to_fp32(ctx):
+    """Error against the FP64 oracle relative to plain FP32's, normal(0,1) inputs.
+
+    tf32x3 and bf16x6 keep ~24 significand bits per operand and match FP32;
+    bf16x3 keeps ~16 and is about ten times worse (still 100x inside the
+    0.05 percent verify threshold)."""
+    n = 512
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((n, n)).astype(np.float32)
+    B = rng.standard_normal((n, n)).astype(np.float32)
+    C = rng.standard_normal((n, n)).astype(np.float32)
+    ref = oracle.gemm_f64(A, B, C, 1.0, 1.0)
+    err = {p: oracle.error_norms(run_gemm(ctx, A, B, C, 1.0, 1.0, prec=p), ref)[1]
+           for p in [Precision.FP32] + FORMS}
+    print({p.name: f"{e:.3e}" for p, e in err.items()})
+    f32 = err[Precision.FP32]
+    assert err[Precision.TF32X3] < 3 * f32
+    assert err[Precision.BF16X6] < 3 * f32
+    assert err[Precision.BF16X3] < 30 * f32
+
+
+def test_beta_zero_does_not_read_c(ctx):
+    rng = np.random.default_rng(1)
+    A = rng.uniform(-1, 1, (130, 70)).astype(np.float32)
+    B = rng.uniform(-1, 1, (70, 260)).astype(np.float32)
+    C = np.full((130, 260), np.nan, np.float32)
+    dev = run_gemm(ctx, A, B, C, 2.0, 0.0)
+    assert np.isfinite(dev).all()
+    assert oracle.error_norms(dev, oracle.gemm_f64(A, B, None, 2.0, 0.0))[1] < 2e-5
+
+
+@pytest.mark.parametrize("prec", VERIFYING)
+@pytest.mark.parametrize("n", [64, 257, 512])
+def test_syrk_polybench_init_passes_reference_verify(ctx, prec, n):
+    A, C = oracle.init_syrk(n)
+    dA, dC = ctx.upload(A), ctx.upload(C)
+    ctx.syrk(prec, n, n, 123.0, dA, n, 14512.0, dC, n)
+    ctx.synchronize()
+    assert_verify(oracle.host_syrk(n), ctx.download(dC, C.shape))
+
+
+@pytest.mark.parametrize("prec", VERIFYING)
+@pytest.mark.parametrize("n", [64, 257, 512])
+def test_syr2k_polybench_init_passes_reference_verify(ctx, prec, n):
+    A, B, C = oracle.init_syr2k(n)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.syr2k(prec, n, n, 1.0, dA, n, dB, n, 1.0, dC, n)
+    ctx.synchronize()
+    assert_verify(oracle.host_syr2k(n), ctx.download(dC, C.shape))
+
+
+@pytest.mark.parametrize("prec", FORMS)
+@pytest.mark.parametrize("nk", [(128, 64), (300, 200)])
+def test_syr2k_random_vs_fp64(ctx, prec, nk):
+    n, k = nk
+    rng = np.random.default_rng(n + k)
+    A = rng.standard_normal((n, k)).astype(np.float32)
+    B = rng.standard_normal((n, k)).astype(np.float32)
+    C = rng.standard_normal((n, n)).astype(np.float32)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.syr2k(prec, n, k, 0.75, dA, k, dB, k, 1.25, dC, n)
+    ctx.synchronize()
+    ref = oracle.gemm_f64(A, B, C, 0.75, 1.25, op_b=1, A2=B, B2=A)
+    assert oracle.error_norms(ctx.download(dC, C.shape), ref)[1] < frob_bound(prec, 2 * k)
+
+
+@pytest.mark.parametrize("prec", VERIFYING)
+def test_2mm_chain_passes_reference_verify(ctx, prec):
+    P = prec
+    n = 256
+    A, B, C, D = oracle.init_mm2(n)
+    dA, dB, dC, dD = (ctx.upload(x) for x in (A, B, C, D))
+    dE = ctx.alloc(n * n * 4)
+    ctx.gemm(P, n, n, n, 1.0, dA, n, dB, n, 1.0, dC, n)
+    ctx.gemm(P, n, n, n, 1.0, dC, n, dD, n, 0.0, dE, n)
+    ctx.synchronize()
+    assert_verify(oracle.host_mm2(n), ctx.download(dE, (n, n)))
