@@ -1,0 +1,138 @@
+// Driver around one of the reference's own PolyBench sources (TEST
+// INFRASTRUCTURE, built by oracle/build_ref.sh into oracle/_ref/).
+//
+// The reference file is included unmodified with its main() renamed, and
+// compiled against the host-only SYCL stand-in in oracle/sycl_shim.  For a
+// size n the driver writes, as raw float32 row-major files:
+//   <out>_host.f32    the reference's host verification loop result
+//                     (gemm(), mm2_cpu(), mm3_cpu(), syrk(), syr2k())
+//   <out>_device.f32  the output buffer after the reference's run() kernels
+//                     executed on the host (its --device=cpu semantics)
+// and prints "verify=PASS|FAIL" from the reference's own verify().
+// With --main it instead runs the reference's main() with the remaining
+// arguments (its CLI, result consumers and timing harness).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <sycl/sycl.hpp>
+
+#define main reference_main
+#include REF_SOURCE
+#undef main
+
+namespace {
+
+void write_f32(const std::string& path, const float* p, size_t n) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if(!f) {
+    std::perror(path.c_str());
+    std::exit(2);
+  }
+  std::fwrite(p, sizeof(float), n, f);
+  std::fclose(f);
+}
+
+BenchmarkArgs make_args(size_t n) {
+  std::string size = "--size=" + std::to_string(n);
+  const char* argv[] = {"ref", size.c_str(), "--device=cpu", "--num-runs=1"};
+  return BenchmarkCommandLine{4, const_cast<char**>(argv)}.getBenchmarkArgs();
+}
+
+// Output buffer of the benchmark object: the k-th buffer created by setup().
+const float* device_output(size_t first_buffer, size_t index) {
+  auto& log = sycl::detail::buffer_log();
+  return static_cast<const float*>(log.at(first_buffer + index)->data);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if(argc >= 2 && std::strcmp(argv[1], "--main") == 0) {
+    argv[1] = argv[0];
+    return reference_main(argc - 1, argv + 1);
+  }
+  if(argc < 3) {
+    std::fprintf(stderr, "usage: %s <n> <out-prefix> | --main <reference args...>\n", argv[0]);
+    return 2;
+  }
+  const size_t n = std::strtoull(argv[1], nullptr, 10);
+  const std::string out = argv[2];
+  const size_t nn = n * n;
+
+  // 1) host verification loop, on freshly initialised inputs
+  std::vector<float> host_out(nn);
+#if defined(REF_GEMM)
+  {
+    std::vector<float> A(nn), B(nn), C(nn);
+    init(A.data(), B.data(), C.data(), n);
+    gemm(A.data(), B.data(), C.data(), n);
+    host_out = C;
+  }
+  using Bench = Polybench_Gemm;
+  const size_t out_index = 2;
+#elif defined(REF_2MM)
+  {
+    std::vector<float> A(nn), B(nn), C(nn), D(nn), E(nn);
+    init_array(A.data(), B.data(), C.data(), D.data(), n);
+    mm2_cpu(A.data(), B.data(), C.data(), D.data(), E.data(), n);
+    host_out = E;
+  }
+  using Bench = Polybench_2mm;
+  const size_t out_index = 4;
+#elif defined(REF_3MM)
+  {
+    std::vector<float> A(nn), B(nn), C(nn), D(nn), E(nn), F(nn), G(nn);
+    init_array(A.data(), B.data(), C.data(), D.data(), n);
+    mm3_cpu(A.data(), B.data(), C.data(), D.data(), E.data(), F.data(), G.data(), n);
+    host_out = G;
+  }
+  using Bench = Polybench_3mm;
+  const size_t out_index = 6;
+#elif defined(REF_SYRK)
+  {
+    std::vector<float> A(nn), C(nn);
+    init_arrays(A.data(), C.data(), n);
+    syrk(A.data(), C.data(), n);
+    host_out = C;
+  }
+  using Bench = Polybench_Syrk;
+  const size_t out_index = 1;
+#elif defined(REF_SYR2K)
+  {
+    std::vector<float> A(nn), B(nn), C(nn);
+    init_arrays(A.data(), B.data(), C.data(), n);
+    syr2k(A.data(), B.data(), C.data(), n);
+    host_out = C;
+  }
+  using Bench = Polybench_Syr2k;
+  const size_t out_index = 2;
+#else
+#error "define one of REF_GEMM REF_2MM REF_3MM REF_SYRK REF_SYR2K"
+#endif
+  write_f32(out + "_host.f32", host_out.data(), nn);
+
+  // 2) the benchmark's own setup / run / verify with the kernels on the host
+  BenchmarkArgs args = make_args(n);
+  Bench b(args);
+  const size_t first = sycl::detail::buffer_log().size();
+  b.setup();
+  std::vector<sycl::event> events;
+  const auto t0 = std::chrono::steady_clock::now();
+  b.run(events);
+  args.device_queue.wait_and_throw();
+  const auto t1 = std::chrono::steady_clock::now();
+  write_f32(out + "_device.f32", device_output(first, out_index), nn);
+  VerificationSetting vs{true, {0, 0, 0}, {1, 1, 1}};
+  const bool ok = b.verify(vs);
+  std::printf("verify=%s kernel_seconds=%.6f\n", ok ? "PASS" : "FAIL",
+      std::chrono::duration<double>(t1 - t0).count());
+  return 0;
+}

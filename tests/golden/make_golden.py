@@ -1,0 +1,57 @@
+"""Generate the golden fixtures from the reference itself.
+
+Runs the reference's own PolyBench sources, built by oracle/build_ref.sh
+against the host-only SYCL stand-in (this needs the reference sources on the
+machine), and stores:
+
+  reference_outputs.npz   for each benchmark and size n:
+                            <bench>_<n>_host    its host verification loop result
+                            <bench>_<n>_device  its run() kernels' output (host execution)
+  reference_stdout_gemm.txt  its main() output with --output=stdio
+  reference_csv_gemm.txt     its main() output with --output=<csv file> (two flushes)
+
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF_BIN = ROOT / "oracle" / "_ref"
+BENCHES = ["gemm", "2mm", "3mm", "syrk", "syr2k"]
+SIZES = [1, 2, 7, 16, 37, 64]
+
+
+def main() -> None:
+    subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True)
+    arrays = {}
+    with tempfile.TemporaryDirectory() as td:
+        for b in BENCHES:
+            for n in SIZES:
+                prefix = os.path.join(td, f"{b}_{n}")
+                r = subprocess.run([str(REF_BIN / f"ref_{b}"), str(n), prefix], check=True, capture_output=True,
+                                   text=True)
+                if "verify=PASS" not in r.stdout:
+                    sys.exit(f"reference verify failed for {b} n={n}: {r.stdout}")
+                for kind in ("host", "device"):
+                    arrays[f"{b}_{n}_{kind}"] = np.fromfile(f"{prefix}_{kind}.f32", np.float32).reshape(n, n)
+        np.savez_compressed(HERE / "reference_outputs.npz", **arrays)
+
+        out = subprocess.run([str(REF_BIN / "ref_gemm"), "--main", "--size=16", "--num-runs=3"], check=True,
+                             capture_output=True, text=True).stdout
+        (HERE / "reference_stdout_gemm.txt").write_text(out)
+        csv = os.path.join(td, "out.csv")
+        for _ in range(2):
+            subprocess.run([str(REF_BIN / "ref_gemm"), "--main", "--size=16", "--num-runs=2", f"--output={csv}"],
+                           check=True, capture_output=True)
+        (HERE / "reference_csv_gemm.txt").write_text(Path(csv).read_text())
+    print("wrote", HERE / "reference_outputs.npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""The drop-in executables' harness on the host device (--device=cpu): CLI,
+result formats against the reference's own output, verification paths.
+No GPU: the host device runs the reference kernel bodies on the CPU cores.
+"""
+import json
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+BIN = ROOT / "sycl-bench_gb300" / "bin"
+GOLDEN = ROOT / "tests" / "golden"
+BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3mm", "syrk": "Polybench_Syrk",
+           "syr2k": "Polybench_Syr2k"}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def executables():
+    import sys
+    sys.path.insert(0, str(ROOT / "sycl-bench_gb300"))
+    import build
+    build.build_lib()
+    build.build_executables()
+
+
+def run(bench, *args, cwd=None):
+    r = subprocess.run([str(BIN / f"polybench_{bench}"), *args], capture_output=True, text=True, cwd=cwd,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    return r
+
+
+def stdout_keys(text):
+    return [ln.split(":", 1)[0] for ln in text.splitlines() if ln and not ln.startswith("*")]
+
+
+@pytest.mark.parametrize("bench", list(BENCHES))
+def test_host_device_run_verifies(bench):
+    out = run(bench, "--size=48", "--device=cpu", "--num-runs=2").stdout
+    blocks = out.split("**********")
+    assert f"Results for {BENCHES[bench]}" in out
+    assert out.count("Verification: PASS") == 2, out   # FP32 and the fp64 variant
+    assert f"Results for {BENCHES[bench]}_fp64" in out
+
+
+def test_stdout_result_names_match_reference():
+    ref = (GOLDEN / "reference_stdout_gemm.txt").read_text()
+    ours = run("gemm", "--size=16", "--num-runs=3", "--device=cpu", "--precision=fp32").stdout
+    first = ours.split("********** Results for Polybench_Gemm_fp64")[0]
+    assert stdout_keys(first) == stdout_keys(ref)
+    assert first.splitlines()[0] == ref.splitlines()[0]
+
+
+def test_csv_columns_match_reference(tmp_path):
+    ref_lines = (GOLDEN / "reference_csv_gemm.txt").read_text().splitlines()
+    csv = tmp_path / "out.csv"
+    run("gemm", "--size=16", "--num-runs=2", "--device=cpu", f"--output={csv}")
+    lines = csv.read_text().splitlines()
+    assert lines[0] == ref_lines[0]                         # identical header
+    row = lines[1].split(",")
+    assert row[0] == "Polybench_Gemm"
+    # same number of fields (samples are one quoted field without commas)
+    assert len(row) == len(ref_lines[1].split(","))
+    header = lines[0].split(",")
+    cell = dict(zip(header[1:], row[1:]))
+    assert cell["Verification"] == "PASS" and cell["problem-size"] == "16" and cell["local-size"] == "256"
+    assert re.fullmatch(r'"[0-9. ]+"', cell["run-time-samples"])
+    assert lines[2] == ref_lines[0]                         # a header per flush, as the reference
+    assert lines[3].startswith("Polybench_Gemm_fp64,")
+
+
+def test_no_verification_reports_na():
+    out = run("syrk", "--size=16", "--device=cpu", "--no-verification", "--num-runs=1").stdout
+    assert "Verification: N/A" in out and "PASS" not in out
+
+
+def test_throughput_metric_is_sp_gflop():
+    out = run("gemm", "--size=32", "--device=cpu", "--num-runs=1").stdout
+    m = re.search(r"throughput-metric: ([0-9.]+) \[SP GFLOP\]", out)
+    assert m and float(m.group(1)) == pytest.approx(2 * 32 ** 3 / 2 ** 30, rel=2e-2)
+
+
+def test_warmup_run_is_not_recorded():
+    out = run("gemm", "--size=16", "--device=cpu", "--num-runs=3", "--warmup-run").stdout
+    samples = re.search(r'run-time-samples: "([^"]*)"', out).group(1).split()
+    assert len(samples) == 3
+
+
+def test_duplicate_argument_is_reported():
+    r = run("gemm", "--size=16", "--size=32", "--device=cpu")
+    assert "several times" in r.stderr
+
+
+def test_unknown_device_and_precision_are_reported():
+    assert "unknown device type" in run("gemm", "--size=16", "--device=fpga").stderr
+    assert "unknown --precision" in run("gemm", "--size=16", "--device=cpu", "--precision=fp7").stderr
+
+
+def test_error_report_and_variants(tmp_path):
+    rep = tmp_path / "err.jsonl"
+    out = run("syr2k", "--size=40", "--device=cpu", "--num-runs=2", "--init=normal", "--seed=7",
+              f"--error-report={rep}").stdout
+    assert "Results for Polybench_Syr2k_normal_seed7" in out
+    lines = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert len(lines) == 4  # two runs x (fp32, fp64)
+    assert all(x["init"] == "normal" and x["seed"] == 7 for x in lines)
+    fp32 = [x for x in lines if x["benchmark"] == "Polybench_Syr2k_normal_seed7"]
+    assert fp32 and all(x["frob_rel"] < 1e-5 for x in fp32)
+
+
+def test_fp64_oracle_verification_mode():
+    out = run("3mm", "--size=24", "--device=cpu", "--num-runs=1", "--verification-oracle=fp64").stdout
+    assert out.count("Verification: PASS") == 2
+
+
+def test_alpha_beta_variant_name():
+    out = run("syrk", "--size=16", "--device=cpu", "--num-runs=1", "--alpha=32412", "--beta=2123").stdout
+    assert "Results for Polybench_Syrk_ab32412_2123" in out
+    assert "Verification: PASS" in out
