@@ -1,0 +1,53 @@
+"""The five drop-in executables on the GPU: every precision form verifies
+with the reference's own host loop, CSV columns are the reference's, and the
+CUDA-event kernel timings are filled."""
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+BIN = ROOT / "sycl-bench_gb300" / "bin"
+GOLDEN = ROOT / "tests" / "golden"
+BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3mm", "syrk": "Polybench_Syrk",
+           "syr2k": "Polybench_Syr2k"}
+
+
+def run(bench, *args):
+    r = subprocess.run([str(BIN / f"polybench_{bench}"), *args], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "rror" not in r.stderr, r.stderr
+    return r.stdout
+
+
+@pytest.mark.parametrize("bench", list(BENCHES))
+def test_all_forms_verify_on_gpu(bench):
+    out = run(bench, "--size=320", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6")
+    names = re.findall(r"Results for (\S+?)\*", out)
+    base = BENCHES[bench]
+    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6", base + "_fp64"]
+    assert out.count("Verification: PASS") == 5, out
+    assert "kernel-time-mean: N/A" not in out
+    assert "NVIDIA" in out or "GB" in out  # device-name is the CUDA device
+
+
+def test_csv_columns_match_reference_on_gpu(tmp_path):
+    csv = tmp_path / "o.csv"
+    run("gemm", "--size=1024", "--num-runs=3", f"--output={csv}")
+    lines = csv.read_text().splitlines()
+    assert lines[0] == (GOLDEN / "reference_csv_gemm.txt").read_text().splitlines()[0]
+    cell = dict(zip(lines[0].split(",")[1:], lines[1].split(",")[1:]))
+    assert cell["Verification"] == "PASS"
+    assert float(cell["kernel-time-min"]) > 0 and float(cell["kernel-time-min"]) <= float(cell["run-time-min"])
+
+
+def test_fp64_oracle_and_error_report_on_gpu(tmp_path):
+    rep = tmp_path / "e.jsonl"
+    out = run("syr2k", "--size=512", "--num-runs=1", "--precision=fp32,bf16x3", "--init=normal",
+              "--verification-oracle=fp64", f"--error-report={rep}")
+    assert out.count("Verification: PASS") == 3
+    lines = rep.read_text().splitlines()
+    assert len(lines) == 3
