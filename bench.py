@@ -181,7 +181,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     def fresh_c():
         ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(dC), gbpoly._ptr(dC0), nbytes)
 
-    forms = [Precision.FP32, Precision.BF16X3]
+    forms = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.TF32]
     headline = Precision.BF16X3
     tiers = {}
     sampler = ClockSampler(dist.local_rank)
@@ -271,14 +271,17 @@ def run_gpu(args, dist: Dist) -> dict | None:
                 "frac": kernel_tflops / peak, "traffic": None,
                 "peak_source": f"computed: {props['sm_count']} SMs x 128 FFMA lanes x 2 x {clk_mhz:.0f} MHz"}
     else:
-        # split-BF16 runs 3 BF16 MMAs per algorithmic multiply-add: its ceiling is the BF16 peak / 3
+        # BF16-MMA equivalents per algorithmic multiply-add (a TF32 MMA runs at half the BF16 rate):
+        # bf16x3 3, tf32x3 and bf16x6 6, tf32 2.  The form's ceiling is the BF16 peak divided by that.
+        mma_per_mac = {Precision.BF16X3: 3, Precision.TF32X3: 6, Precision.BF16X6: 6, Precision.TF32: 2}[headline]
         bf16 = peaks["bf16_tflops"]
-        peak = bf16 / 3.0
+        peak = bf16 / mma_per_mac
         roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": kernel_tflops / peak, "traffic": TRAFFIC_PER_LAUNCH.get((head["dominant_kernel"], n)),
                 "kernel": head["dominant_kernel"], "kernel_avg_ms": head["dominant_avg_ms"],
-                "peak_source": f"{bf16} TFLOP/s dense BF16 burst ({peak_kind}) / 3 MMAs per multiply-add",
-                "frac_of_bf16_peak_tensor_work": 3 * kernel_tflops / bf16}
+                "peak_source": f"{bf16} TFLOP/s dense BF16 burst ({peak_kind}) / {mma_per_mac} BF16 MMAs per "
+                               f"multiply-add",
+                "frac_of_bf16_peak_tensor_work": mma_per_mac * kernel_tflops / bf16}
     ctx.close()
     return {
         "value": head["tflops"], "ms_per_step": head["ms_per_step"], "tiers": tiers, "clocks": clocks,

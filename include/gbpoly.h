@@ -99,6 +99,28 @@ gbpoly_status gbpoly_memcpy_d2h(gbpoly_ctx* ctx, void* dst, const void* src, siz
 gbpoly_status gbpoly_memcpy_d2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes);
 gbpoly_status gbpoly_memset(gbpoly_ctx* ctx, void* dst, int value, size_t bytes);
 
+/* Make the context workspace (split panels of the tensor-core forms) at
+ * least `bytes` large now, so that later calls of that size do not allocate.
+ * Needed before capturing tensor-core calls into a graph.  Synchronises. */
+gbpoly_status gbpoly_workspace_reserve(gbpoly_ctx* ctx, size_t bytes);
+/* Workspace bytes a contraction of this shape and form needs (0 for fp32). */
+gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, int same_operand,
+    size_t* bytes);
+
+/* ----------------------------------------------------------------- graphs -- */
+
+/* Capture the work later calls queue on the context's stream into a CUDA
+ * graph, then replay it with one launch.  This is how the multi-kernel
+ * benchmarks (2mm.cpp:94-123, 3mm.cpp:115-158, which the reference submits as
+ * separate command groups) run as one launch.  Between begin and end no call
+ * may allocate: reserve the workspace first (a tensor-core call that would
+ * grow it returns GBPOLY_ERR_STATE). */
+typedef struct gbpoly_graph gbpoly_graph;
+gbpoly_status gbpoly_graph_begin(gbpoly_ctx* ctx);
+gbpoly_status gbpoly_graph_end(gbpoly_ctx* ctx, gbpoly_graph** graph);
+gbpoly_status gbpoly_graph_launch(gbpoly_ctx* ctx, gbpoly_graph* graph);
+gbpoly_status gbpoly_graph_destroy(gbpoly_ctx* ctx, gbpoly_graph* graph);
+
 /* ----------------------------------------------------------------- events -- */
 
 /* Event handles for kernel-time profiling.  They replace the

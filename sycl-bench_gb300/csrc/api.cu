@@ -31,6 +31,10 @@ gbpoly_status cuda_fail(cudaError_t e, const char* what) {
 
 gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) {
   if(ctx->ws.bytes >= bytes) return GBPOLY_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GBPOLY_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
+  if(cs != cudaStreamCaptureStatusNone)
+    return fail(GBPOLY_ERR_STATE, "workspace would grow during graph capture; call gbpoly_workspace_reserve first");
   if(ctx->ws.ptr) {
     GBPOLY_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     GBPOLY_CUDA_TRY(cudaFree(ctx->ws.ptr));
@@ -122,6 +126,11 @@ gbpoly_status check_matrix(const char* name, const void* p, int64_t rows, int64_
 
 struct gbpoly_event {
   cudaEvent_t ev = nullptr;
+};
+
+struct gbpoly_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
 };
 
 extern "C" {
@@ -258,6 +267,60 @@ gbpoly_status gbpoly_profile_read(gbpoly_ctx* ctx, int max_entries, char* names,
     counts[i] = cnt[i];
     total_ms[i] = tot[i];
   }
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_workspace_reserve(gbpoly_ctx* ctx, size_t bytes) {
+  CTX_TRY(ctx);
+  return ensure_workspace(ctx, bytes);
+}
+
+gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, int same_operand,
+    size_t* bytes) {
+  if(!bytes || M < 0 || N < 0 || K < 0) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  *bytes = workspace_bytes(prec, M, N, K, same_operand != 0);
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_graph_begin(gbpoly_ctx* ctx) {
+  CTX_TRY(ctx);
+  GBPOLY_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_graph_end(gbpoly_ctx* ctx, gbpoly_graph** out) {
+  CTX_TRY(ctx);
+  if(!out) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GBPOLY_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
+  if(cs != cudaStreamCaptureStatusActive) return fail(GBPOLY_ERR_STATE, "no graph capture in progress");
+  auto* g = new gbpoly_graph();
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g->graph);
+  if(e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if(e != cudaSuccess) {
+    if(g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return cuda_fail(e, "graph capture");
+  }
+  *out = g;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_graph_launch(gbpoly_ctx* ctx, gbpoly_graph* g) {
+  CTX_TRY(ctx);
+  if(!g || !g->exec) return fail(GBPOLY_ERR_INVALID, "null graph");
+  ProfileScope prof(ctx, "graph");
+  GBPOLY_CUDA_TRY(cudaGraphLaunch(g->exec, ctx->stream));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_graph_destroy(gbpoly_ctx* ctx, gbpoly_graph* g) {
+  if(!g) return GBPOLY_OK;
+  if(ctx) cudaSetDevice(ctx->device);
+  if(g->exec) cudaGraphExecDestroy(g->exec);
+  if(g->graph) cudaGraphDestroy(g->graph);
+  delete g;
   return GBPOLY_OK;
 }
 

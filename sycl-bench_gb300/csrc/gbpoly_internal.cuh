@@ -119,6 +119,8 @@ gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
 // Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
 // term panels live in the context workspace.
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a);
+// Workspace bytes launch_gemm_tensor needs for this shape (0 for FP32).
+size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same_operand);
 
 // ---------------------------------------------------------------- device side
 

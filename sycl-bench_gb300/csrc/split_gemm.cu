@@ -13,15 +13,26 @@
 //   * split_kernel (memory bound): writes the K-major term panels of an
 //     operand into the context workspace (transposing through shared memory
 //     when the operand is MN-major), K padded with zeros to the k-block;
-//   * split_gemm_kernel: one 128 x BN tile of C per CTA, warp specialised:
-//       warp 0     TMA producer: the term tiles of A (128 rows) and B (BN rows),
-//                  128-byte rows (64 BF16 or 32 TF32 along K) with 128-byte
-//                  swizzle, into a ring of STAGES shared-memory stages;
-//       warp 1     allocates BN TMEM columns; one lane issues the products'
-//                  tcgen05.mma (M=128, N=BN; K=16 BF16 or K=8 TF32) and
-//                  commits each stage back to the producer;
-//       warps 4-7  epilogue: tcgen05.ld of the accumulator (one TMEM lane
-//                  quarter per warp), C = alpha*acc + beta*C.
+//   * split_gemm_kernel: persistent (one CTA per SM walks 128 x BN tiles of
+//     C), warp specialised, 384 threads:
+//       warp 0      TMA producer: the term tiles of A (128 rows) and B (BN rows),
+//                   128-byte rows (64 BF16 or 32 TF32 along K) with 128-byte
+//                   swizzle, into a ring of STAGES shared-memory stages;
+//       warp 1      allocates 2*BN TMEM columns; one lane issues the products'
+//                   tcgen05.mma (M=128, N=BN; K=16 BF16 or K=8 TF32) into one
+//                   of two TMEM chunk buffers, restarting the accumulator
+//                   every CH stages, and commits stages and chunks;
+//       warps 4-11  epilogue (setmaxnreg 208): each warp owns 32 rows (its
+//                   TMEM lane quarter) x BN/2 columns and sums the chunks in
+//                   FP32 registers with round-to-nearest adds, then writes
+//                   C = alpha*acc + beta*C.
+//     The tensor core accumulates with truncation: over long K its error
+//     grows with the number of MMA steps (measured 3.6e-6 normwise at K=512
+//     for 24-bit operand splits, against 2.6e-7 for the same products summed
+//     with round to nearest).  Each stage therefore starts a fresh TMEM
+//     chunk, issues its cross products before its main product (only the
+//     last BK/KMMA truncating steps see the full-size partial sum), and the
+//     chunks are summed with round to nearest in registers.
 //     syr2k's two products (A_i.B_j^T + B_i.A_j^T) alternate stage by stage
 //     into the same accumulator.
 // All mbarrier waits are bounded (gbpoly_internal.cuh).
@@ -45,7 +56,15 @@ struct Form {
   static constexpr int A_TILE = BM * 128, B_TILE = BN * 128;
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
-  static constexpr uint32_t TMEM_COLS = BN;
+  // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
+  // accumulation inside the tensor core stays short); chunks are summed in
+  // FP32 registers, round to nearest, by the epilogue warps.  Two chunk
+  // buffers in TMEM so the MMAs run ahead of the epilogue.
+  static constexpr int CH = 1;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;
+  static constexpr int HALF = BN / 2;  // columns per epilogue warp
+  static constexpr int THREADS = 384;  // warpgroup 0: producer, MMA; warpgroups 1-2: epilogue
+  static constexpr uint32_t REGS_CTRL = 56, REGS_EPI = 208;
   static constexpr uint32_t IDESC =
       umma::InstrDesc<BM, BN, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
   static_assert(SMEM <= 232448, "shared memory");
@@ -150,28 +169,33 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
 }
 
 template <class F>
-__global__ void __launch_bounds__(256, 1) split_gemm_kernel(const __grid_constant__ GemmMaps maps, int npair, int M,
-    int N, int Kp, float alpha, float beta, float* __restrict__ C, int64_t ldc, int* err) {
+__global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_constant__ GemmMaps maps, int npair,
+    int M, int N, int Kp, float alpha, float beta, float* __restrict__ C, int64_t ldc, int* err) {
   extern __shared__ __align__(1024) char smem_raw[];
   char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + F::STAGES * F::STAGE);
   uint64_t* empty = full + F::STAGES;
-  uint64_t* accum = empty + F::STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* chunk_full = empty + F::STAGES;  // [2]
+  uint64_t* chunk_empty = chunk_full + 2;    // [2]
+  uint64_t* drain = chunk_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_m = (M + F::BM - 1) / F::BM, tiles_n = (N + F::BN - 1) / F::BN;
-  int tile_m, tile_n;
-  tile_coords(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
-  const int m0 = tile_m * F::BM, n0 = tile_n * F::BN;
-  const int iters = (Kp / F::BK) * npair;
+  const int tiles = tiles_m * tiles_n;
+  const int iters = (Kp / F::BK) * npair;           // stage iterations per tile
+  const int chunks = (iters + F::CH - 1) / F::CH;    // TMEM chunks per tile
 
   if(threadIdx.x == 0) {
     for(int s = 0; s < F::STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for(int b = 0; b < 2; ++b) {
+      mbar_init(&chunk_full[b], 1);
+      mbar_init(&chunk_empty[b], 8);  // one arrival per epilogue warp
+    }
+    mbar_init(drain, 1);
     fence_mbar_init();
   }
   if(warp == 1) {
@@ -183,96 +207,147 @@ __global__ void __launch_bounds__(256, 1) split_gemm_kernel(const __grid_constan
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  if(warp == 0) {
-    // ------------------------------------------------------------ producer
-    if(lane == 0) {
+  if(warp < 4) {
+    umma::regs_decrease<F::REGS_CTRL>();
+    if(warp == 0 && lane == 0) {
+      // ---------------------------------------------------------- producer
       for(int p = 0; p < npair; ++p)
         for(int t = 0; t < F::terms; ++t) {
           tma_prefetch_desc(&maps.p[p].l[t]);
           tma_prefetch_desc(&maps.p[p].r[t]);
         }
-      int issued = 0;
-      for(int it = 0; it < iters; ++it) {
-        const int s = it % F::STAGES;
-        if(it >= F::STAGES && !mbar_wait(&empty[s], ((it / F::STAGES) - 1) & 1, err, kDevErrEmptyWait)) break;
-        const ProductMaps& pm = maps.p[it % npair];
-        const int k0 = (it / npair) * F::BK;
-        char* st = smem + s * F::STAGE;
-        mbar_arrive_expect_tx(&full[s], F::STAGE);
+      int g = 0;  // global stage iteration across tiles
+      bool ok = true;
+      for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        int tile_m, tile_n;
+        tile_coords(tile, tiles_m, tiles_n, tile_m, tile_n);
+        const int m0 = tile_m * F::BM, n0 = tile_n * F::BN;
+        for(int it = 0; it < iters; ++it, ++g) {
+          const int s = g % F::STAGES;
+          if(g >= F::STAGES && !mbar_wait(&empty[s], ((g / F::STAGES) - 1) & 1, err, kDevErrEmptyWait)) {
+            ok = false;
+            break;
+          }
+          const ProductMaps& pm = maps.p[it % npair];
+          const int k0 = (it / npair) * F::BK;
+          char* st = smem + s * F::STAGE;
+          mbar_arrive_expect_tx(&full[s], F::STAGE);
 #pragma unroll
-        for(int t = 0; t < F::terms; ++t) {
-          tma_load_2d(st + t * F::A_TILE, &pm.l[t], &full[s], k0, m0);
-          tma_load_2d(st + F::terms * F::A_TILE + t * F::B_TILE, &pm.r[t], &full[s], k0, n0);
+          for(int t = 0; t < F::terms; ++t) {
+            tma_load_2d(st + t * F::A_TILE, &pm.l[t], &full[s], k0, m0);
+            tma_load_2d(st + F::terms * F::A_TILE + t * F::B_TILE, &pm.r[t], &full[s], k0, n0);
+          }
         }
-        ++issued;
       }
-      for(int it = max(0, issued - F::STAGES); it < issued; ++it)
-        if(!mbar_wait(&full[it % F::STAGES], (it / F::STAGES) & 1, err, kDevErrDrainWait)) break;
-    }
-  } else if(warp == 1) {
-    // ------------------------------------------------------------ MMA issue
-    if(lane == 0) {
-      for(int it = 0; it < iters; ++it) {
-        const int s = it % F::STAGES;
-        if(!mbar_wait(&full[s], (it / F::STAGES) & 1, err, kDevErrFullWait)) break;
-        umma::fence_after_sync();
-        const uint32_t a_base = smem_u32(smem + s * F::STAGE);
-        const uint32_t b_base = a_base + F::terms * F::A_TILE;
+      // do not leave while copies into this CTA's shared memory are in flight
+      for(int h = max(0, g - F::STAGES); h < g; ++h)
+        if(!mbar_wait(&full[h % F::STAGES], (h / F::STAGES) & 1, err, kDevErrDrainWait)) break;
+    } else if(warp == 1 && lane == 0) {
+      // ------------------------------------------------------- MMA issue
+      int g = 0, chunk = 0;
+      bool ok = true;
+      for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        for(int it = 0; it < iters && ok; ++it, ++g) {
+          const int b = chunk & 1;
+          if(it % F::CH == 0) {
+            // the epilogue must have drained this chunk buffer (used two chunks ago)
+            if(chunk >= 2 && !mbar_wait(&chunk_empty[b], ((chunk >> 1) - 1) & 1, err, kDevErrMmaWait)) {
+              ok = false;
+              break;
+            }
+            umma::fence_after_sync();
+          }
+          const int s = g % F::STAGES;
+          if(!mbar_wait(&full[s], (g / F::STAGES) & 1, err, kDevErrFullWait)) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t d = tmem + uint32_t(b * F::BN);
+          const uint32_t a_base = smem_u32(smem + s * F::STAGE);
+          const uint32_t b_base = a_base + F::terms * F::A_TILE;
+          // Issue order: every cross product (p >= 1) of the stage first, the
+          // main product (p = 0) last, so the truncating accumulation runs on
+          // a small partial sum for all but the last BK/KMMA steps.
+          constexpr int KSTEPS = F::BK / F::KMMA;
 #pragma unroll
-        for(int k = 0; k < F::BK / F::KMMA; ++k) {
-          const uint32_t off = k * 32;  // 32 bytes of K per MMA
-#pragma unroll
-          for(int p = 0; p < F::nprod; ++p) {
+          for(int q = 0; q < F::nprod * KSTEPS; ++q) {
+            const int p = (q / KSTEPS + 1) % F::nprod;
+            const int k = q % KSTEPS;
+            const uint32_t off = k * 32;  // 32 bytes of K per MMA
             const uint64_t da = umma::desc_k_sw128(a_base + prod_a(p) * F::A_TILE + off);
             const uint64_t db = umma::desc_k_sw128(b_base + prod_b(p) * F::B_TILE + off);
-            const uint32_t acc = (it > 0 || k > 0 || p > 0) ? 1u : 0u;
+            const uint32_t acc = (it % F::CH != 0 || q > 0) ? 1u : 0u;
             if constexpr(F::elem == Elem::BF16)
-              umma::mma_f16(tmem, da, db, F::IDESC, acc);
+              umma::mma_f16(d, da, db, F::IDESC, acc);
             else
-              umma::mma_tf32(tmem, da, db, F::IDESC, acc);
+              umma::mma_tf32(d, da, db, F::IDESC, acc);
+          }
+          umma::commit(&empty[s]);  // stage s is free once these MMAs have read it
+          if(it % F::CH == F::CH - 1 || it == iters - 1) {
+            umma::commit(&chunk_full[b]);  // chunk complete in TMEM buffer b
+            ++chunk;
           }
         }
-        umma::commit(&empty[s]);  // stage s is free once these MMAs have read it
       }
-      umma::commit(accum);  // accumulator complete (after an error: all issued MMAs drained)
+      umma::commit(drain);  // every MMA issued by this thread has completed
+      mbar_wait(drain, 0, err, kDevErrDrainWait);
     }
-  } else if(warp >= 4) {
+  } else {
     // ------------------------------------------------------------- epilogue
-    const int q = warp & 3;
-    const bool ok = mbar_wait(accum, 0, err, kDevErrMmaWait);
-    umma::fence_after_sync();
-    if(ok) {
-      const int m = m0 + 32 * q + lane;
-      float* crow = C + int64_t(m) * ldc;
-      const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
-#pragma unroll 1
-      for(int c = 0; c < F::BN / 32; ++c) {
-        uint32_t r[32];
-        umma::tmem_ld_32x32b_x32(tmem + (uint32_t(32 * q) << 16) + uint32_t(32 * c), r);
-        umma::tmem_ld_wait();
-        const int n = n0 + 32 * c;
-        if(m >= M || n >= N) continue;
-        if(vec && n + 32 <= N) {
+    umma::regs_increase<F::REGS_EPI>();
+    const int q = warp & 3;          // TMEM lane quarter of this warp
+    const int h = (warp - 4) >> 2;   // column half
+    const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+    float acc[F::HALF];
+    int chunk = 0;
+    bool ok = true;
+    for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+      int tile_m, tile_n;
+      tile_coords(tile, tiles_m, tiles_n, tile_m, tile_n);
+      const int m = tile_m * F::BM + 32 * q + lane;
+      const int nbase = tile_n * F::BN + h * F::HALF;
+      for(int c = 0; c < chunks; ++c, ++chunk) {
+        const int b = chunk & 1;
+        if(!mbar_wait(&chunk_full[b], (chunk >> 1) & 1, err, kDevErrMmaWait)) {
+          ok = false;
+          break;
+        }
+        umma::fence_after_sync();
+        const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b * F::BN + h * F::HALF);
 #pragma unroll
-          for(int j = 0; j < 32; j += 4) {
-            float4 o = make_float4(alpha * __uint_as_float(r[j]), alpha * __uint_as_float(r[j + 1]),
-                alpha * __uint_as_float(r[j + 2]), alpha * __uint_as_float(r[j + 3]));
-            if(beta != 0.f) {
-              const float4 cv = *reinterpret_cast<const float4*>(crow + n + j);
-              o.x = fmaf(beta, cv.x, o.x);
-              o.y = fmaf(beta, cv.y, o.y);
-              o.z = fmaf(beta, cv.z, o.z);
-              o.w = fmaf(beta, cv.w, o.w);
-            }
-            *reinterpret_cast<float4*>(crow + n + j) = o;
+        for(int j = 0; j < F::HALF / 32; ++j) {
+          uint32_t r[32];
+          umma::tmem_ld_32x32b_x32(base + 32 * j, r);
+          umma::tmem_ld_wait();
+#pragma unroll
+          for(int i = 0; i < 32; ++i) acc[32 * j + i] = (c == 0) ? __uint_as_float(r[i]) : acc[32 * j + i] + __uint_as_float(r[i]);
+        }
+        umma::fence_before_sync();
+        __syncwarp();
+        if(lane == 0) mbar_arrive(&chunk_empty[b]);
+      }
+      if(!ok || m >= M) continue;
+      float* crow = C + int64_t(m) * ldc + nbase;
+      if(vec && nbase + F::HALF <= N) {
+#pragma unroll
+        for(int j = 0; j < F::HALF; j += 4) {
+          float4 o = make_float4(alpha * acc[j], alpha * acc[j + 1], alpha * acc[j + 2], alpha * acc[j + 3]);
+          if(beta != 0.f) {
+            const float4 cv = *reinterpret_cast<const float4*>(crow + j);
+            o.x = fmaf(beta, cv.x, o.x);
+            o.y = fmaf(beta, cv.y, o.y);
+            o.z = fmaf(beta, cv.z, o.z);
+            o.w = fmaf(beta, cv.w, o.w);
           }
-        } else {
+          *reinterpret_cast<float4*>(crow + j) = o;
+        }
+      } else {
 #pragma unroll
-          for(int j = 0; j < 32; ++j) {
-            if(n + j < N) {
-              const float v = alpha * __uint_as_float(r[j]);
-              crow[n + j] = (beta != 0.f) ? fmaf(beta, crow[n + j], v) : v;
-            }
+        for(int j = 0; j < F::HALF; ++j) {
+          if(nbase + j < N) {
+            const float v = alpha * acc[j];
+            crow[j] = (beta != 0.f) ? fmaf(beta, crow[j], v) : v;
           }
         }
       }
@@ -283,8 +358,6 @@ __global__ void __launch_bounds__(256, 1) split_gemm_kernel(const __grid_constan
   __syncthreads();
   if(warp == 1) {
     umma::fence_after_sync();
-    if(lane == 0) mbar_wait(accum, 0, err, kDevErrDrainWait);  // no MMA may still write TMEM
-    __syncwarp();
     umma::tmem_dealloc(tmem, F::TMEM_COLS);
   }
 }
@@ -325,18 +398,38 @@ gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, i
   return GBPOLY_OK;
 }
 
+// Workspace layout: terms x [A panel] then terms x [B panel] (B absent when
+// both operands are the same rows).
+struct Layout {
+  int64_t Kp;
+  size_t a_stride, b_stride, a_bytes, b_bytes;
+};
+
+template <class F>
+Layout layout(int64_t M, int64_t N, int64_t K, bool same) {
+  Layout l;
+  l.Kp = align_up(size_t(std::max<int64_t>(K, 1)), 64);
+  l.a_stride = align_up(size_t(M) * l.Kp * F::esz, 1024);
+  l.b_stride = align_up(size_t(N) * l.Kp * F::esz, 1024);
+  l.a_bytes = F::terms * l.a_stride;
+  l.b_bytes = same ? 0 : F::terms * l.b_stride;
+  return l;
+}
+
+// syrk: both operands are the rows of A; split once
+bool same_operand(const GemmF32Args& a) {
+  return !a.dual && a.A == a.B && a.op_a == GBPOLY_OP_N && a.op_b == GBPOLY_OP_T && a.lda == a.ldb && a.M == a.N;
+}
+
 template <class F>
 gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel_name) {
   if(a.M == 0 || a.N == 0) return GBPOLY_OK;
   if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
     return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");
-  const int64_t Kp = align_up(size_t(std::max<int64_t>(a.K, 1)), 64);
-  // syrk: both operands are the rows of A; split once
-  const bool same = !a.dual && a.A == a.B && a.op_a == GBPOLY_OP_N && a.op_b == GBPOLY_OP_T && a.lda == a.ldb &&
-                    a.M == a.N;
-  const size_t a_stride = align_up(size_t(a.M) * Kp * F::esz, 1024);
-  const size_t b_stride = align_up(size_t(a.N) * Kp * F::esz, 1024);
-  const size_t a_bytes = F::terms * a_stride, b_bytes = same ? 0 : F::terms * b_stride;
+  const bool same = same_operand(a);
+  const Layout lay = layout<F>(a.M, a.N, a.K, same);
+  const int64_t Kp = lay.Kp;
+  const size_t a_stride = lay.a_stride, b_stride = lay.b_stride, a_bytes = lay.a_bytes, b_bytes = lay.b_bytes;
   gbpoly_status st = ensure_workspace(ctx, a_bytes + b_bytes);
   if(st != GBPOLY_OK) return st;
   char* ws = static_cast<char*>(ctx->ws.ptr);
@@ -363,17 +456,42 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   static unsigned attr_set = 0;
   if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
     GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
+    // setmaxnreg redistributes the registers the CTA was launched with: the
+    // split must fit in threads x registers-per-thread at launch, or the
+    // increase would wait forever.
+    cudaFuncAttributes fa;
+    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F>));
+    const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
+    if(long(fa.numRegs) * F::THREADS < need)
+      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
     attr_set |= 1u << ctx->device;
   }
   const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
   ProfileScope prof(ctx, kernel_name);
-  split_gemm_kernel<F><<<static_cast<unsigned>(tiles), 256, F::SMEM, ctx->stream>>>(maps, npair, int(a.M), int(a.N),
-      int(Kp), a.alpha, a.beta, a.C, a.ldc, ctx->err_dev);
+  split_gemm_kernel<F><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(maps, npair, int(a.M), int(a.N), int(Kp), a.alpha,
+      a.beta, a.C, a.ldc, ctx->err_dev);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
 }
 
+template <class F>
+size_t bytes_of(int64_t M, int64_t N, int64_t K, bool same) {
+  const Layout l = layout<F>(M, N, K, same);
+  return l.a_bytes + l.b_bytes;
+}
+
 }  // namespace
+
+size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same) {
+  switch(prec) {
+  case GBPOLY_PREC_TF32: return bytes_of<FormTF32>(M, N, K, same);
+  case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same);
+  case GBPOLY_PREC_TF32X3: return bytes_of<FormTF32x3>(M, N, K, same);
+  case GBPOLY_PREC_BF16X6: return bytes_of<FormBF16x6>(M, N, K, same);
+  default: return 0;
+  }
+}
 
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
   switch(prec) {

@@ -73,6 +73,12 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_memcpy_d2h": (ct.c_int, [_vp, _vp, _vp, ct.c_size_t]),
     "gbpoly_memcpy_d2d": (ct.c_int, [_vp, _vp, _vp, ct.c_size_t]),
     "gbpoly_memset": (ct.c_int, [_vp, _vp, ct.c_int, ct.c_size_t]),
+    "gbpoly_workspace_reserve": (ct.c_int, [_vp, ct.c_size_t]),
+    "gbpoly_workspace_query": (ct.c_int, [ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_int, ct.POINTER(ct.c_size_t)]),
+    "gbpoly_graph_begin": (ct.c_int, [_vp]),
+    "gbpoly_graph_end": (ct.c_int, [_vp, ct.POINTER(_vp)]),
+    "gbpoly_graph_launch": (ct.c_int, [_vp, _vp]),
+    "gbpoly_graph_destroy": (ct.c_int, [_vp, _vp]),
     "gbpoly_event_create": (ct.c_int, [_vp, ct.POINTER(_vp)]),
     "gbpoly_event_destroy": (ct.c_int, [_vp, _vp]),
     "gbpoly_event_record": (ct.c_int, [_vp, _vp]),
@@ -263,6 +269,28 @@ class Context:
             nm = names.raw[64 * i:64 * i + 64].split(b"\0", 1)[0].decode()
             out[nm] = (counts[i], tot[i])
         return out
+
+    def workspace_reserve(self, nbytes: int) -> None:
+        _check(self.lib.gbpoly_workspace_reserve(self.handle, nbytes))
+
+    def workspace_query(self, prec, M, N, K, same_operand=False) -> int:
+        v = ct.c_size_t()
+        _check(self.lib.gbpoly_workspace_query(int(prec), M, N, K, 1 if same_operand else 0, ct.byref(v)))
+        return int(v.value)
+
+    def graph_begin(self) -> None:
+        _check(self.lib.gbpoly_graph_begin(self.handle))
+
+    def graph_end(self):
+        g = _vp()
+        _check(self.lib.gbpoly_graph_end(self.handle, ct.byref(g)))
+        return g
+
+    def graph_launch(self, g) -> None:
+        _check(self.lib.gbpoly_graph_launch(self.handle, g))
+
+    def graph_destroy(self, g) -> None:
+        _check(self.lib.gbpoly_graph_destroy(self.handle, g))
 
     def event(self) -> Event:
         return Event(self)
