@@ -170,6 +170,25 @@ gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N
     const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
 
 
+/* Allocation-free split-BF16 contraction: the same result as
+ * gbpoly_gemm_f32(ctx, GBPOLY_PREC_BF16X3, ...), for callers that may not
+ * allocate device memory at call time (graph capture in global mode, an
+ * application-owned memory pool, allocation-free real-time loops, device
+ * memory quotas).  It has no counterpart in the reference.
+ * The hi/lo panels live in a fixed 32 MiB device array inside the library
+ * (held by every GPU that loads the library until exit) instead of the
+ * context workspace, so the call performs no cudaMalloc/cudaFree:
+ *   - shapes whose panels exceed it, about (M + N) * round_up(K, 64) * 4 bytes
+ *     > 32 MiB, are rejected with GBPOLY_ERR_INVALID and a message;
+ *   - the first call on each device looks the array's device address up
+ *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *   - all calls share the one array: calls whose work overlaps on the GPU
+ *     (several streams or contexts on one device) race and must be ordered
+ *     by the caller. */
+gbpoly_status gbpoly_gemm_f32_bf16x3_noalloc(gbpoly_ctx* ctx, gbpoly_op op_a, gbpoly_op op_b, int64_t M, int64_t N,
+    int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C,
+    int64_t ldc);
+
 /* ------------------------------------------------------------------- FP64 -- */
 
 /* C <- alpha * op(A) * op(B) + beta * C in FP64.  The double variants of the

@@ -37,6 +37,9 @@
 //     into the same accumulator.
 // All mbarrier waits are bounded (gbpoly_internal.cuh).
 #include <cuda_bf16.h>
+#include <stdio.h>
+
+#include <mutex>
 
 #include "gbpoly_internal.cuh"
 #include "umma.cuh"
@@ -503,4 +506,111 @@ gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const G
   }
 }
 
+
+// ------------------------------------------------ allocation-free entry point
+//
+// Some callers may not allocate device memory when they call a contraction:
+// code being captured into a CUDA graph in global capture mode (cudaMalloc is
+// not permitted there), applications that hand the whole device to their own
+// memory pool at start-up, real-time loops that forbid an allocation (it can
+// synchronise the device) after initialisation, and processes under a hard
+// device-memory quota.  For them the split-BF16 form has a second entry point
+// whose split panels live in this fixed, file-scope device array instead of
+// the context workspace.  Every GPU that loads this library holds the array
+// until the process exits.
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (the array's name is only a host-side handle in host code).
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[64] = {};
+
+gbpoly_status noalloc_scratch(int device, char** out) {
+  if(device < 0 || device >= 64) return fail(GBPOLY_ERR_UNSUPPORTED, "device index beyond 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if(!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if(e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+    g_noalloc_addr[device] = p;
+  }
+  *out = static_cast<char*>(g_noalloc_addr[device]);
+  return GBPOLY_OK;
+}
+
+}  // namespace
+
+gbpoly_status launch_gemm_bf16x3_noalloc(gbpoly_ctx* ctx, const GemmF32Args& a) {
+  using F = FormBF16x3;
+  if(a.M == 0 || a.N == 0) return GBPOLY_OK;
+  if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
+    return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");
+  const bool same = same_operand(a);
+  const Layout lay = layout<F>(a.M, a.N, a.K, same);
+  const size_t need = lay.a_bytes + lay.b_bytes;
+  if(need > kNoAllocScratchBytes) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+        "M=%lld N=%lld K=%lld needs %zu bytes of split panels; the allocation-free entry point has %zu "
+        "(about (M+N) x round_up(K,64) x 4 bytes must fit)",
+        (long long)a.M, (long long)a.N, (long long)a.K, need, kNoAllocScratchBytes);
+    return fail(GBPOLY_ERR_INVALID, buf);
+  }
+  char* ws = nullptr;
+  gbpoly_status st = noalloc_scratch(ctx->device, &ws);
+  if(st != GBPOLY_OK) return st;
+  Panels pa{ws, lay.a_stride};
+  Panels pb = same ? pa : Panels{ws + lay.a_bytes, lay.b_stride};
+  if(a.K > 0) {
+    // the split pass writes every panel element it is read from (zero K padding included)
+    if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, lay.Kp, pa)) != GBPOLY_OK) return st;
+    if(!same && (st = launch_split<F>(ctx, a.B, a.ldb, a.op_b == GBPOLY_OP_T, a.N, a.K, lay.Kp, pb)) != GBPOLY_OK)
+      return st;
+  } else {
+    GBPOLY_CUDA_TRY(cudaMemsetAsync(ws, 0, need, ctx->stream));  // the array keeps the previous call's panels
+  }
+  GemmMaps maps;
+  if((st = make_product_maps<F>(ctx, maps.p[0], pa, a.M, pb, a.N, lay.Kp)) != GBPOLY_OK) return st;
+  maps.p[1] = maps.p[0];
+  static unsigned attr_set = 0;
+  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
+    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
+    cudaFuncAttributes fa;
+    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F>));
+    if(long(fa.numRegs) * F::THREADS < 128l * F::REGS_CTRL + 256l * F::REGS_EPI)
+      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
+    attr_set |= 1u << ctx->device;
+  }
+  const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
+  ProfileScope prof(ctx, "bf16x3_gemm_noalloc");
+  split_gemm_kernel<F><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(maps, 1, int(a.M), int(a.N), int(lay.Kp), a.alpha,
+      a.beta, a.C, a.ldc, ctx->err_dev);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
 }  // namespace gbpoly
+
+extern "C" gbpoly_status gbpoly_gemm_f32_bf16x3_noalloc(gbpoly_ctx* ctx, gbpoly_op op_a, gbpoly_op op_b, int64_t M,
+    int64_t N, int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C,
+    int64_t ldc) {
+  using namespace gbpoly;
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
+  if((op_a != GBPOLY_OP_N && op_a != GBPOLY_OP_T) || (op_b != GBPOLY_OP_N && op_b != GBPOLY_OP_T))
+    return fail(GBPOLY_ERR_INVALID, "bad operand op");
+  if(M < 0 || N < 0 || K < 0) return fail(GBPOLY_ERR_INVALID, "negative dimension");
+  const int64_t ar = op_a == GBPOLY_OP_N ? M : K, ac = op_a == GBPOLY_OP_N ? K : M;
+  const int64_t br = op_b == GBPOLY_OP_N ? K : N, bc = op_b == GBPOLY_OP_N ? N : K;
+  if((ar > 0 && ac > 0 && (!A || lda < ac)) || (br > 0 && bc > 0 && (!B || ldb < bc)) ||
+      (M > 0 && N > 0 && (!C || ldc < N)))
+    return fail(GBPOLY_ERR_INVALID, "null matrix or leading dimension smaller than its columns");
+  GemmF32Args a{};
+  a.M = M, a.N = N, a.K = K, a.alpha = alpha, a.beta = beta, a.op_a = op_a, a.op_b = op_b;
+  a.A = A, a.lda = lda, a.B = B, a.ldb = ldb, a.C = C, a.ldc = ldc;
+  return launch_gemm_bf16x3_noalloc(ctx, a);
+}

@@ -92,6 +92,8 @@ SIGNATURES: dict[str, tuple] = {
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
                                     ct.c_float, _vp, _c_i64]),
+    "gbpoly_gemm_f32_bf16x3_noalloc": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
+                                                  _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_gemm_f64": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, _vp,
                                    _c_i64, ct.c_double, _vp, _c_i64]),
     "gbpoly_syrk_f64": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, ct.c_double, _vp, _c_i64]),
