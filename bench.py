@@ -35,7 +35,9 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of the same kernel and workload (profiles/ holds the summaries).
-TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {}
+# N=4096 capture: 389.6e6 bytes per bf16x3 launch (profiles/split_gemm_bf16x3_gemm_n4096.md); the N=8192
+# figure scales it by the panel bytes each tile streams (8x the FLOPs, 4x the matrix bytes): x4.
+TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {("bf16x3_gemm", 4096): 389.6e6, ("bf16x3_gemm", 8192): 4 * 389.6e6}
 
 
 # ------------------------------------------------------------------ helpers
