@@ -189,6 +189,10 @@ def run_gpu(args, dist: Dist) -> dict | None:
     sampler = ClockSampler(dist.local_rank)
     sampler.start()
     timed_window = (0.0, 0.0)
+    tuned = {}
+    for prec in forms:
+        if prec != Precision.FP32:  # tile configuration from the autotuner, before any timing
+            tuned[prec] = ctx.autotune(prec, n, n, n, reps=3)[0]
     for prec in forms:
         fresh_c()
         one(prec)
@@ -224,6 +228,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
             "kernels": {k: {"launches": c, "avg_ms": t / c, "share": t / sum(x[1] for x in kernels.values())}
                         for k, (c, t) in kernels.items()},
             "dominant_kernel": top[0], "dominant_avg_ms": top[1][1] / top[1][0],
+            "tile_config": tuned.get(prec),
         }
         ev0.destroy()
         ev1.destroy()

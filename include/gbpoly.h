@@ -107,6 +107,26 @@ gbpoly_status gbpoly_workspace_reserve(gbpoly_ctx* ctx, size_t bytes);
 gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, int same_operand,
     size_t* bytes);
 
+/* -------------------------------------------------------------- autotuner -- */
+
+/* Each tensor-core form has a few compiled tile configurations (tile width,
+ * K bytes per pipeline stage, pipeline depth).  The context keeps one per
+ * (form, ceil(log2) of M, N, K) -- configuration 0 unless tuned or set. */
+gbpoly_status gbpoly_gemm_config_count(gbpoly_precision prec, int* count);
+gbpoly_status gbpoly_gemm_config_set(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K,
+    int config);
+gbpoly_status gbpoly_gemm_config_get(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K,
+    int* config);
+/* Times every configuration of `prec` on an M x N x K problem (allocates its
+ * own operands), `reps` launches each, keeps the fastest for that shape
+ * bucket and returns it.  Synchronous. */
+gbpoly_status gbpoly_autotune_gemm(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K, int reps,
+    int* best_config, float* best_ms);
+/* Persist / restore the tuned table as text lines keyed by device name and
+ * driver version (entries of other devices in the file are kept). */
+gbpoly_status gbpoly_autotune_save(gbpoly_ctx* ctx, const char* path);
+gbpoly_status gbpoly_autotune_load(gbpoly_ctx* ctx, const char* path, int* loaded);
+
 /* ----------------------------------------------------------------- graphs -- */
 
 /* Capture the work later calls queue on the context's stream into a CUDA

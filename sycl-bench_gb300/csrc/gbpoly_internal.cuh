@@ -12,7 +12,9 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/gbpoly.h"
@@ -61,6 +63,8 @@ struct gbpoly_ctx {
   bool profiling = false;
   std::vector<gbpoly::ProfileRecord> prof;        // launches since the last read
   std::vector<cudaEvent_t> event_pool;            // reusable events
+  // tile configuration per (form, log2-bucket of M, N, K), from the autotuner
+  std::map<std::tuple<int, int, int, int>, int> tuned;
 };
 
 namespace gbpoly {
@@ -119,6 +123,12 @@ gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
 // Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
 // term panels live in the context workspace.
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a);
+// Tile configurations of a tensor-core form (0 for none); launch with an
+// explicit configuration; the configuration the context uses for a shape.
+int tensor_config_count(gbpoly_precision prec);
+gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, int config, const GemmF32Args& a);
+int tuned_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
+std::tuple<int, int, int, int> shape_bucket(gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
 // Workspace bytes launch_gemm_tensor needs for this shape (0 for FP32).
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same_operand);
 

@@ -49,21 +49,22 @@ namespace {
 
 enum class Elem { BF16, TF32 };
 
-template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_>
+template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128>
 struct Form {
   static constexpr Elem elem = E;
   static constexpr int terms = TERMS, nprod = NPROD, BM = 128, BN = BN_, STAGES = STAGES_;
+  static constexpr int ROW = ROW_;                       // bytes of K per smem row (= swizzle width)
   static constexpr int esz = E == Elem::BF16 ? 2 : 4;
-  static constexpr int BK = 128 / esz;                 // elements per 128-byte row
-  static constexpr int KMMA = E == Elem::BF16 ? 16 : 8; // K of one tcgen05.mma (32 bytes)
-  static constexpr int A_TILE = BM * 128, B_TILE = BN * 128;
+  static constexpr int BK = ROW / esz;                   // K elements per stage
+  static constexpr int KMMA = E == Elem::BF16 ? 16 : 8;  // K of one tcgen05.mma (32 bytes)
+  static constexpr int A_TILE = BM * ROW, B_TILE = BN * ROW;
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
   // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
   // accumulation inside the tensor core stays short); chunks are summed in
   // FP32 registers, round to nearest, by the epilogue warps.  Two chunk
   // buffers in TMEM so the MMAs run ahead of the epilogue.
-  static constexpr int CH = 1;
+  static constexpr int CH = 128 / ROW;
   static constexpr uint32_t TMEM_COLS = 2 * BN;
   static constexpr int HALF = BN / 2;  // columns per epilogue warp
   static constexpr int THREADS = 384;  // warpgroup 0: producer, MMA; warpgroups 1-2: epilogue
@@ -71,12 +72,22 @@ struct Form {
   static constexpr uint32_t IDESC =
       umma::InstrDesc<BM, BN, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
   static_assert(SMEM <= 232448, "shared memory");
+  static_assert(TMEM_COLS <= 512, "tensor memory");
 };
 
+// Tile configurations per form (index = config id).  Config 0 is the default.
 using FormTF32 = Form<Elem::TF32, 1, 1, 256, 4>;
+using FormTF32_b = Form<Elem::TF32, 1, 1, 256, 8, 64>;
+using FormTF32_c = Form<Elem::TF32, 1, 1, 128, 6>;
 using FormBF16x3 = Form<Elem::BF16, 2, 3, 256, 2>;
+using FormBF16x3_b = Form<Elem::BF16, 2, 3, 256, 4, 64>;
+using FormBF16x3_c = Form<Elem::BF16, 2, 3, 128, 3>;
 using FormTF32x3 = Form<Elem::TF32, 2, 3, 256, 2>;
+using FormTF32x3_b = Form<Elem::TF32, 2, 3, 256, 4, 64>;
+using FormTF32x3_c = Form<Elem::TF32, 2, 3, 128, 3>;
 using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
+using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
+using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 3, 64>;
 
 // Term indices of product p: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 ? 1 : (p == 4 ? 1 : (p == 5 ? 2 : 0)); }
@@ -278,8 +289,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             const int p = (q / KSTEPS + 1) % F::nprod;
             const int k = q % KSTEPS;
             const uint32_t off = k * 32;  // 32 bytes of K per MMA
-            const uint64_t da = umma::desc_k_sw128(a_base + prod_a(p) * F::A_TILE + off);
-            const uint64_t db = umma::desc_k_sw128(b_base + prod_b(p) * F::B_TILE + off);
+            const uint64_t da = umma::desc_k<F::ROW>(a_base + prod_a(p) * F::A_TILE + off);
+            const uint64_t db = umma::desc_k<F::ROW>(b_base + prod_b(p) * F::B_TILE + off);
             const uint32_t acc = (it % F::CH != 0 || q > 0) ? 1u : 0u;
             if constexpr(F::elem == Elem::BF16)
               umma::mma_f16(d, da, db, F::IDESC, acc);
@@ -388,7 +399,7 @@ template <class F>
 gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, int64_t left_rows, Panels right,
     int64_t right_rows, int64_t Kp) {
   const auto dt = F::elem == Elem::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  const auto sw = CU_TENSOR_MAP_SWIZZLE_128B;
+  const auto sw = F::ROW == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
   gbpoly_status st;
   for(int t = 0; t < F::terms; ++t) {
     if((st = make_tmap_2d(ctx, &pm.l[t], dt, F::esz, left.base + t * left.stride, left_rows, Kp, Kp, F::BM, F::BK,
@@ -487,6 +498,7 @@ size_t bytes_of(int64_t M, int64_t N, int64_t K, bool same) {
 }  // namespace
 
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same) {
+  // the largest over the configurations of the form (they differ only in padding)
   switch(prec) {
   case GBPOLY_PREC_TF32: return bytes_of<FormTF32>(M, N, K, same);
   case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same);
@@ -496,16 +508,37 @@ size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, b
   }
 }
 
-gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
+int tensor_config_count(gbpoly_precision prec) {
   switch(prec) {
-  case GBPOLY_PREC_TF32: return run_form<FormTF32>(ctx, a, "tf32_gemm");
-  case GBPOLY_PREC_BF16X3: return run_form<FormBF16x3>(ctx, a, "bf16x3_gemm");
-  case GBPOLY_PREC_TF32X3: return run_form<FormTF32x3>(ctx, a, "tf32x3_gemm");
-  case GBPOLY_PREC_BF16X6: return run_form<FormBF16x6>(ctx, a, "bf16x6_gemm");
-  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available");
+  case GBPOLY_PREC_TF32:
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_TF32X3:
+  case GBPOLY_PREC_BF16X6: return 3;
+  default: return 0;
   }
 }
 
+gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, int config, const GemmF32Args& a) {
+  switch(prec * 8 + config) {
+  case GBPOLY_PREC_TF32 * 8 + 0: return run_form<FormTF32>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 1: return run_form<FormTF32_b>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 2: return run_form<FormTF32_c>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form<FormBF16x3>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form<FormBF16x3_b>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form<FormBF16x3_c>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form<FormTF32x3>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form<FormTF32x3_b>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form<FormTF32x3_c>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form<FormBF16x6>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form<FormBF16x6_b>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form<FormBF16x6_c>(ctx, a, "bf16x6_gemm");
+  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
+  }
+}
+
+gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
+  return launch_gemm_tensor_config(ctx, prec, tuned_config(ctx, prec, a.M, a.N, a.K), a);
+}
 
 // ------------------------------------------------ allocation-free entry point
 //

@@ -36,6 +36,27 @@ __device__ __forceinline__ uint64_t desc_k_sw128(uint32_t smem_addr) {
   return d;
 }
 
+// Same for 64-byte rows written with 64-byte swizzle (8-row atoms of 512 bytes).
+__device__ __forceinline__ uint64_t desc_k_sw64(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((smem_addr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>(1) << 16;           // LBO (unused)
+  d |= static_cast<uint64_t>(512 >> 4) << 32;    // SBO: 8 rows x 64 B
+  d |= static_cast<uint64_t>(1) << 46;           // version
+  d |= static_cast<uint64_t>(4) << 61;           // SWIZZLE_64B
+  return d;
+}
+
+// K-major swizzled operand descriptor for ROW-byte rows (128 or 64).
+template <int ROW>
+__device__ __forceinline__ uint64_t desc_k(uint32_t smem_addr) {
+  static_assert(ROW == 128 || ROW == 64, "row bytes");
+  if constexpr(ROW == 128)
+    return desc_k_sw128(smem_addr);
+  else
+    return desc_k_sw64(smem_addr);
+}
+
 enum class AbType : uint32_t { F16 = 0, BF16 = 1, TF32 = 2 };
 
 template <int M, int N, AbType T>

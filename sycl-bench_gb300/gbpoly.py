@@ -75,6 +75,13 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_memset": (ct.c_int, [_vp, _vp, ct.c_int, ct.c_size_t]),
     "gbpoly_workspace_reserve": (ct.c_int, [_vp, ct.c_size_t]),
     "gbpoly_workspace_query": (ct.c_int, [ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_int, ct.POINTER(ct.c_size_t)]),
+    "gbpoly_gemm_config_count": (ct.c_int, [ct.c_int, ct.POINTER(ct.c_int)]),
+    "gbpoly_gemm_config_set": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_int]),
+    "gbpoly_gemm_config_get": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, _c_i64, ct.POINTER(ct.c_int)]),
+    "gbpoly_autotune_gemm": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_int, ct.POINTER(ct.c_int),
+                                        ct.POINTER(ct.c_float)]),
+    "gbpoly_autotune_save": (ct.c_int, [_vp, ct.c_char_p]),
+    "gbpoly_autotune_load": (ct.c_int, [_vp, ct.c_char_p, ct.POINTER(ct.c_int)]),
     "gbpoly_graph_begin": (ct.c_int, [_vp]),
     "gbpoly_graph_end": (ct.c_int, [_vp, ct.POINTER(_vp)]),
     "gbpoly_graph_launch": (ct.c_int, [_vp, _vp]),
@@ -279,6 +286,32 @@ class Context:
         v = ct.c_size_t()
         _check(self.lib.gbpoly_workspace_query(int(prec), M, N, K, 1 if same_operand else 0, ct.byref(v)))
         return int(v.value)
+
+    def config_count(self, prec) -> int:
+        v = ct.c_int()
+        _check(self.lib.gbpoly_gemm_config_count(int(prec), ct.byref(v)))
+        return v.value
+
+    def config_set(self, prec, M, N, K, config: int) -> None:
+        _check(self.lib.gbpoly_gemm_config_set(self.handle, int(prec), M, N, K, config))
+
+    def config_get(self, prec, M, N, K) -> int:
+        v = ct.c_int()
+        _check(self.lib.gbpoly_gemm_config_get(self.handle, int(prec), M, N, K, ct.byref(v)))
+        return v.value
+
+    def autotune(self, prec, M, N, K, reps: int = 3) -> tuple[int, float]:
+        c, ms = ct.c_int(), ct.c_float()
+        _check(self.lib.gbpoly_autotune_gemm(self.handle, int(prec), M, N, K, reps, ct.byref(c), ct.byref(ms)))
+        return c.value, ms.value
+
+    def autotune_save(self, path) -> None:
+        _check(self.lib.gbpoly_autotune_save(self.handle, str(path).encode()))
+
+    def autotune_load(self, path) -> int:
+        n = ct.c_int()
+        _check(self.lib.gbpoly_autotune_load(self.handle, str(path).encode(), ct.byref(n)))
+        return n.value
 
     def graph_begin(self) -> None:
         _check(self.lib.gbpoly_graph_begin(self.handle))
