@@ -114,9 +114,12 @@ private:
 };
 
 // What a command group sees: where it runs.
+class Queue;
+
 class Handler {
 public:
   explicit Handler(DeviceImpl* d) : dev(d) {}
+  explicit Handler(const Queue& q);
   bool on_host() const { return dev->host; }
   gbpoly_ctx* ctx() const { return dev->ctx; }
 
@@ -188,6 +191,8 @@ public:
     return ev;
   }
 
+  DeviceImpl* impl_ptr() const { return impl.get(); }
+
 private:
   static std::string host_cpu_name();
   std::shared_ptr<DeviceImpl> impl;
@@ -197,6 +202,8 @@ private:
 
 #include <cstdlib>
 #include <fstream>
+
+inline gb::Handler::Handler(const Queue& q) : dev(q.impl_ptr()) {}
 
 inline std::string gb::Queue::host_cpu_name() {
   std::ifstream f("/proc/cpuinfo");

@@ -42,7 +42,12 @@ template <class T>
 class Polybench_2mm {
 public:
   Polybench_2mm(const BenchmarkArgs& args, gbpoly_precision prec = GBPOLY_PREC_FP32)
-      : args(args), size(args.problem_size), opt(poly::options(args, prec)) {}
+      : args(args), size(args.problem_size), opt(poly::options(args, prec)),
+        use_graph(args.cli.isFlagSet("--graph") && !args.device_queue.is_host()) {}
+
+  ~Polybench_2mm() {
+    if(graph) gbpoly_graph_destroy(args.device_queue.ctx(), graph);
+  }
 
   void setup() {
     const size_t nn = size * size;
@@ -57,17 +62,19 @@ public:
     C_buffer.initialize(args.device_queue, C.data(), nn);
     D_buffer.initialize(args.device_queue, D.data(), nn);
     E_buffer.initialize(args.device_queue, E.data(), nn);
+    if(use_graph) capture_stages();
   }
 
   void run(std::vector<gb::Event>& events) {
+    if(use_graph) {  // both stages as one graph launch
+      events.push_back(args.device_queue.submit(
+          [&](gb::Handler& h) { gb::check(gbpoly_graph_launch(h.ctx(), graph), "graph launch"); }));
+      return;
+    }
     // C += A.B   (2mm.cpp:99-106)
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) {
-      contract(h, A_buffer.get(), B_buffer.get(), T(1), C_buffer.get());
-    }));
+    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage1(h); }));
     // E = C.D    (2mm.cpp:114-122)
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) {
-      contract(h, C_buffer.get(), D_buffer.get(), T(0), E_buffer.get());
-    }));
+    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage2(h); }));
   }
 
   bool verify(VerificationSetting&) {
@@ -93,7 +100,9 @@ public:
     return ok;
   }
 
-  std::string getBenchmarkName(const BenchmarkArgs&) const { return poly::variant_name<T>("Polybench_2mm", opt); }
+  std::string getBenchmarkName(const BenchmarkArgs&) const {
+    return poly::variant_name<T>("Polybench_2mm", opt) + (use_graph ? "_graph" : "");
+  }
 
   static ThroughputMetric getThroughputMetric(const BenchmarkArgs& args) {
     const double n = double(args.problem_size);
@@ -101,6 +110,25 @@ public:
   }
 
 private:
+  void stage1(gb::Handler& h) { contract(h, A_buffer.get(), B_buffer.get(), T(1), C_buffer.get()); }
+  void stage2(gb::Handler& h) { contract(h, C_buffer.get(), D_buffer.get(), T(0), E_buffer.get()); }
+
+  // --graph: record both stages into one CUDA graph (untimed, in setup)
+  void capture_stages() {
+    gbpoly_ctx* ctx = args.device_queue.ctx();
+    if constexpr(std::is_same<T, float>::value) {
+      size_t ws = 0;
+      const int64_t n = int64_t(size);
+      gb::check(gbpoly_workspace_query(opt.precision, n, n, n, 0, &ws), "workspace query");
+      gb::check(gbpoly_workspace_reserve(ctx, ws), "workspace reserve");
+    }
+    gb::Handler h(args.device_queue);
+    gb::check(gbpoly_graph_begin(ctx), "graph begin");
+    stage1(h);
+    stage2(h);
+    gb::check(gbpoly_graph_end(ctx, &graph), "graph end");
+  }
+
   // out = a.b + beta*out on the queue's device
   void contract(gb::Handler& h, const T* a, const T* b, T beta, T* out) {
     if(h.on_host()) {
@@ -148,6 +176,8 @@ private:
   BenchmarkArgs args;
   const size_t size;
   poly::Options opt;
+  bool use_graph;
+  gbpoly_graph* graph = nullptr;
   std::vector<T> A, B, C, D, E;
   PrefetchedBuffer<T, 2> A_buffer, B_buffer, C_buffer, D_buffer, E_buffer;
 };

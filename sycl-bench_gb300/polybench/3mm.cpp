@@ -51,7 +51,12 @@ template <class T>
 class Polybench_3mm {
 public:
   Polybench_3mm(const BenchmarkArgs& args, gbpoly_precision prec = GBPOLY_PREC_FP32)
-      : args(args), size(args.problem_size), opt(poly::options(args, prec)) {}
+      : args(args), size(args.problem_size), opt(poly::options(args, prec)),
+        use_graph(args.cli.isFlagSet("--graph") && !args.device_queue.is_host()) {}
+
+  ~Polybench_3mm() {
+    if(graph) gbpoly_graph_destroy(args.device_queue.ctx(), graph);
+  }
 
   void setup() {
     const size_t nn = size * size;
@@ -64,18 +69,18 @@ public:
     E_buffer.initialize(args.device_queue, E.data(), nn);
     F_buffer.initialize(args.device_queue, F.data(), nn);
     G_buffer.initialize(args.device_queue, G.data(), nn);
+    if(use_graph) capture_stages();
   }
 
   void run(std::vector<gb::Event>& events) {
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) {  // E = A.B  (3mm.cpp:120-127)
-      contract(h, A_buffer.get(), B_buffer.get(), E_buffer.get());
-    }));
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) {  // F = C.D  (3mm.cpp:135-142)
-      contract(h, C_buffer.get(), D_buffer.get(), F_buffer.get());
-    }));
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) {  // G = E.F  (3mm.cpp:150-157)
-      contract(h, E_buffer.get(), F_buffer.get(), G_buffer.get());
-    }));
+    if(use_graph) {  // the three stages as one graph launch
+      events.push_back(args.device_queue.submit(
+          [&](gb::Handler& h) { gb::check(gbpoly_graph_launch(h.ctx(), graph), "graph launch"); }));
+      return;
+    }
+    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 0); }));  // E = A.B (3mm.cpp:120-127)
+    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 1); }));  // F = C.D (3mm.cpp:135-142)
+    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 2); }));  // G = E.F (3mm.cpp:150-157)
   }
 
   bool verify(VerificationSetting&) {
@@ -101,7 +106,9 @@ public:
     return ok;
   }
 
-  std::string getBenchmarkName(const BenchmarkArgs&) const { return poly::variant_name<T>("Polybench_3mm", opt); }
+  std::string getBenchmarkName(const BenchmarkArgs&) const {
+    return poly::variant_name<T>("Polybench_3mm", opt) + (use_graph ? "_graph" : "");
+  }
 
   static ThroughputMetric getThroughputMetric(const BenchmarkArgs& args) {
     const double n = double(args.problem_size);
@@ -109,6 +116,27 @@ public:
   }
 
 private:
+  void stage(gb::Handler& h, int i) {
+    if(i == 0) contract(h, A_buffer.get(), B_buffer.get(), E_buffer.get());
+    if(i == 1) contract(h, C_buffer.get(), D_buffer.get(), F_buffer.get());
+    if(i == 2) contract(h, E_buffer.get(), F_buffer.get(), G_buffer.get());
+  }
+
+  // --graph: record the three stages into one CUDA graph (untimed, in setup)
+  void capture_stages() {
+    gbpoly_ctx* ctx = args.device_queue.ctx();
+    if constexpr(std::is_same<T, float>::value) {
+      size_t ws = 0;
+      const int64_t n = int64_t(size);
+      gb::check(gbpoly_workspace_query(opt.precision, n, n, n, 0, &ws), "workspace query");
+      gb::check(gbpoly_workspace_reserve(ctx, ws), "workspace reserve");
+    }
+    gb::Handler h(args.device_queue);
+    gb::check(gbpoly_graph_begin(ctx), "graph begin");
+    for(int i = 0; i < 3; ++i) stage(h, i);
+    gb::check(gbpoly_graph_end(ctx, &graph), "graph end");
+  }
+
   void contract(gb::Handler& h, const T* a, const T* b, T* out) {
     if(h.on_host()) {
       poly::host_gemm_body<T>(size, false, T(1), a, b, T(0), out);
@@ -156,6 +184,8 @@ private:
   BenchmarkArgs args;
   const size_t size;
   poly::Options opt;
+  bool use_graph;
+  gbpoly_graph* graph = nullptr;
   std::vector<T> A, B, C, D, E, F, G;
   PrefetchedBuffer<T, 2> A_buffer, B_buffer, C_buffer, D_buffer, E_buffer, F_buffer, G_buffer;
 };

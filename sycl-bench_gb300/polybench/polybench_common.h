@@ -11,6 +11,7 @@
 //      --verification-oracle=host|fp64          host FP32 loop of the reference
 //                                               (default) or an FP64 reference
 //      --error-report=<file.jsonl>              append max/Frobenius error vs FP64
+//      --graph                                  (2mm, 3mm) stages as one captured CUDA graph
 //  * Memoised oracles: the reference recomputes its O(N^3) host loop after
 //    every run (include/common.h:113-121); the result depends only on the
 //    benchmark, size and inputs, so it is computed once per process.

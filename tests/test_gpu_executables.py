@@ -56,3 +56,12 @@ def test_fp64_oracle_and_error_report_on_gpu(tmp_path):
     import json
     rows = [json.loads(x) for x in rep2.read_text().splitlines()]
     assert len(rows) == 3 and all(r["frob_rel"] < 1e-5 for r in rows)
+
+
+@pytest.mark.parametrize("bench", ["2mm", "3mm"])
+def test_graph_mode_verifies(bench):
+    out = run(bench, "--size=512", "--num-runs=3", "--graph", "--precision=fp32,bf16x3")
+    base = BENCHES[bench]
+    names = re.findall(r"Results for (\S+?)\*", out)
+    assert names == [base + "_graph", base + "_bf16x3_graph", base + "_fp64_graph"]
+    assert out.count("Verification: PASS") == 3, out
