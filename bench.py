@@ -267,6 +267,8 @@ def run_gpu(args, dist: Dist) -> dict | None:
     for p in (hA, hB, hC, hOut):
         ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
 
+    grouped = None if args.no_grouped else run_grouped_workload(ctx, args)
+
     head = tiers[headline.name.lower()]
     peaks, peak_kind = load_peaks()
     kernel_tflops = flops / (head["dominant_avg_ms"] * 1e-3) / 1e12
@@ -296,8 +298,98 @@ def run_gpu(args, dist: Dist) -> dict | None:
         "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 * dist.world, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
         "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
-        "device": props, "peak_kind": peak_kind,
+        "device": props, "peak_kind": peak_kind, "grouped": grouped,
     }
+
+
+def run_grouped_workload(ctx, args) -> dict:
+    """512 independent GEMMs C = A.B + 0.5 C, M, N, K log-uniform in [64, 2048]
+    (seed 2024), entries uniform[-1, 1] times a per-matrix scale log-uniform in
+    [1e-3, 1e3]: one grouped tensor-core plan (split pass + one persistent
+    launch) replayed as a CUDA graph, against one plain FP32 launch per GEMM;
+    per-matrix Frobenius error against an FP64 DGEMM on the GPU."""
+    import gbpoly
+    from gbpoly import Precision
+
+    rng = np.random.default_rng(2024)
+    count = args.grouped_count
+    lo, hi = np.log(64), np.log(2048)
+    shapes = [tuple(int(np.exp(rng.uniform(lo, hi))) for _ in range(3)) for _ in range(count)]
+    items, mats = [], []
+    for (M, N, K) in shapes:
+        sc = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e3))))
+        A = (rng.uniform(-1, 1, (M, K)) * sc).astype(np.float32)
+        B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+        C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+        dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+        items.append(dict(M=M, N=N, K=K, alpha=1.0, beta=0.5, A=dA, lda=K, B=dB, ldb=N, C=dC, ldc=N))
+        mats.append((C, dA, dB, dC))
+    flops = float(sum(2 * M * N * K for M, N, K in shapes))
+
+    # FP64 reference per problem (GPU DGEMM), kept on the device
+    refs = []
+    for (M, N, K), (C, dA, dB, dC) in zip(shapes, mats):
+        a64, b64, r64 = ctx.alloc(M * K * 8), ctx.alloc(K * N * 8), ctx.alloc(M * N * 8)
+        ctx.convert_f32_f64(dA, a64, M * K)
+        ctx.convert_f32_f64(dB, b64, K * N)
+        ctx.convert_f32_f64(dC, r64, M * N)
+        ctx.gemm_f64(M, N, K, 1.0, a64, K, b64, N, 0.5, r64, N)
+        ctx.free(a64)
+        ctx.free(b64)
+        refs.append(r64)
+    ctx.synchronize()
+
+    def reset_c():
+        for C, _, _, dC in mats:
+            ctx.h2d(dC, C)
+
+    def errors():
+        e = [ctx.error_norms(dC, N, r, N, M, N)[1] for (M, N, K), (_, _, _, dC), r in zip(shapes, mats, refs)]
+        return {"frob_rel_max": max(e), "frob_rel_median": float(np.median(e))}
+
+    out = {"workload": f"{count} GEMMs C=A.B+0.5C, M,N,K log-uniform [64,2048] seed 2024, per-matrix scale "
+                       f"log-uniform [1e-3,1e3]", "flops_per_step": flops}
+    descs = ctx.descs(items)
+    for prec, mode in ((Precision.FP32, "per-GEMM launches"), (Precision.BF16X3, "grouped plan in a CUDA graph"),
+                       (Precision.BF16X6, "grouped plan in a CUDA graph")):
+        plan = ctx.grouped_plan(prec, descs)
+        reset_c()
+        ctx.grouped_run(plan)
+        ctx.synchronize()
+        err = errors()
+        graph = None
+        if prec != Precision.FP32:
+            ctx.graph_begin()
+            ctx.grouped_run(plan)
+            graph = ctx.graph_end()
+
+        def step():
+            if graph is not None:
+                ctx.graph_launch(graph)
+            else:
+                ctx.grouped_run(plan)
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        e0, e1 = ctx.event(), ctx.event()
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        ctx.synchronize()
+        ms = e0.elapsed_ms(e1) / args.steps
+        out[prec.name.lower()] = {"mode": mode, "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12, **err,
+                                  "launches_per_step": 1 if graph is not None else count}
+        if graph is not None:
+            ctx.graph_destroy(graph)
+        ctx.grouped_destroy(plan)
+    out["speedup_bf16x3_vs_fp32"] = out["bf16x3"]["tflops"] / out["fp32"]["tflops"]
+    for r in refs:
+        ctx.free(r)
+    for _, dA, dB, dC in mats:
+        for b in (dA, dB, dC):
+            ctx.free(b)
+    return out
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -331,6 +423,8 @@ def main() -> None:
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-GEMM workload")
+    ap.add_argument("--grouped-count", type=int, default=512)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist()
@@ -378,7 +472,7 @@ def main() -> None:
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
-                    peaks=res["peak_kind"])
+                    peaks=res["peak_kind"], grouped=res["grouped"])
         print(json.dumps(line))
     dist.close()
 

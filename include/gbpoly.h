@@ -190,6 +190,42 @@ gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N
     const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
 
 
+/* -------------------------------------------------------------- grouped -- */
+
+/* One contraction of a group: C = alpha * op(A) * op(B) + beta * C. */
+typedef struct {
+  gbpoly_op op_a, op_b;
+  int64_t M, N, K;
+  float alpha, beta;
+  const float* A;
+  int64_t lda;
+  const float* B;
+  int64_t ldb;
+  float* C;
+  int64_t ldc;
+} gbpoly_gemm_desc;
+
+/* Many independent contractions of uneven shapes.  The reference runs every
+ * contraction as its own kernel (e.g. the stages of 3mm.cpp:115-158); a
+ * grouped plan runs all of them with the tensor-core forms as one split
+ * pass and one persistent launch over all tiles (fp32: one plain launch per
+ * problem).  gbpoly_grouped_plan validates the descriptors and prepares
+ * everything once (it allocates the term panels and tables and copies them
+ * to the device, synchronously); gbpoly_grouped_run only enqueues launches on
+ * the context's stream and can be captured into a graph; the operands and
+ * outputs must stay at the addresses given to the plan. */
+typedef struct gbpoly_grouped gbpoly_grouped;
+gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
+    gbpoly_grouped** plan);
+gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* plan);
+/* Algorithmic FLOPs (sum of 2MNK), output tiles and device bytes of a plan. */
+gbpoly_status gbpoly_grouped_info(gbpoly_grouped* plan, int64_t* flops, int* tiles, size_t* device_bytes);
+/* Waits for the context's stream, then frees the plan. */
+gbpoly_status gbpoly_grouped_destroy(gbpoly_ctx* ctx, gbpoly_grouped* plan);
+/* Plan, run and destroy in one call (synchronous). */
+gbpoly_status gbpoly_gemm_grouped_f32(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count);
+
 /* Allocation-free split-BF16 contraction: the same result as
  * gbpoly_gemm_f32(ctx, GBPOLY_PREC_BF16X3, ...), for callers that may not
  * allocate device memory at call time (graph capture in global mode, an

@@ -39,7 +39,9 @@
 #include <cuda_bf16.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "gbpoly_internal.cuh"
 #include "umma.cuh"
@@ -123,12 +125,10 @@ struct Term<Elem::TF32> {
 // op(X)[r][k] = X[r*ld + k] (k_major) or X[k*ld + r].  Panels are Kp-strided
 // and `panel_stride` elements apart.
 template <Elem E, int TERMS>
-__global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
-    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride) {
+__device__ __forceinline__ void split_tile(const float* __restrict__ X, int64_t ld, int k_major, int R, int K, int Kp,
+    typename Term<E>::T* __restrict__ out, int64_t panel_stride, int64_t r0, int64_t k0, float (*tile)[65]) {
   using T = typename Term<E>::T;
-  __shared__ float tile[64][65];
   const int tid = threadIdx.x;
-  const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
 #pragma unroll
   for(int e = 0; e < 16; ++e) {
     const int idx = tid + e * 256;
@@ -162,6 +162,43 @@ __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X,
   }
 }
 
+template <Elem E, int TERMS>
+__global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
+    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride) {
+  __shared__ float tile[64][65];
+  split_tile<E, TERMS>(X, ld, k_major, R, K, Kp, out, panel_stride, int64_t(blockIdx.y) * 64,
+      int64_t(blockIdx.x) * 64, tile);
+}
+
+// One operand of a grouped call: its 64x64 blocks are blocks
+// [block_start, block_start + ceil(R/64) * Kp/64) of the grouped split launch.
+struct SplitJob {
+  const float* X;
+  int64_t ld;
+  int k_major, R, K, Kp;
+  void* out;
+  int64_t panel_stride;  // elements
+  int block_start, kblocks;
+};
+
+template <Elem E, int TERMS>
+__global__ void __launch_bounds__(256) grouped_split_kernel(const SplitJob* __restrict__ jobs, int njobs) {
+  __shared__ float tile[64][65];
+  const int b = blockIdx.x;
+  int lo = 0, hi = njobs - 1;  // last job with block_start <= b
+  while(lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if(jobs[mid].block_start <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const SplitJob j = jobs[lo];
+  const int local = b - j.block_start;
+  split_tile<E, TERMS>(j.X, j.ld, j.k_major, j.R, j.K, j.Kp, static_cast<typename Term<E>::T*>(j.out),
+      j.panel_stride, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, tile);
+}
+
 // Tensor maps of one product pairing: left operand terms in 128-row boxes,
 // right operand terms in BN-row boxes.
 struct ProductMaps {
@@ -182,9 +219,56 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
   tile_n = r / gsz;
 }
 
-template <class F>
-__global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_constant__ GemmMaps maps, int npair,
-    int M, int N, int Kp, float alpha, float beta, float* __restrict__ C, int64_t ldc, int* err) {
+// What every warp role needs to know about one output tile.
+struct TileInfo {
+  int m0, n0, M, N, Kp, npair;
+  float alpha, beta;
+  float* C;
+  int64_t ldc;
+  const ProductMaps* maps;  // [npair]
+};
+
+// One contraction: tiles in grouped raster order, tensor maps in the
+// kernel's parameter space.
+template <int BM, int BN>
+struct SingleSched {
+  GemmMaps maps;
+  int npair, M, N, Kp;
+  float alpha, beta;
+  float* C;
+  int64_t ldc;
+  __device__ int count() const { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
+  __device__ TileInfo tile(int t) const {
+    int tm, tn;
+    tile_coords(t, (M + BM - 1) / BM, (N + BN - 1) / BN, tm, tn);
+    return TileInfo{tm * BM, tn * BN, M, N, Kp, npair, alpha, beta, C, ldc, maps.p};
+  }
+};
+
+// A group of independent contractions (problem table and tensor maps in
+// global memory), tiles of all problems in one list ordered by decreasing K.
+struct GroupProblem {
+  int M, N, Kp, pad;
+  float alpha, beta;
+  float* C;
+  int64_t ldc;
+};
+template <int BM, int BN>
+struct GroupedSched {
+  const GroupProblem* probs;
+  const ProductMaps* maps;  // one per problem
+  const int4* tiles;        // (problem, tile_m, tile_n, 0)
+  int ntiles;
+  __device__ int count() const { return ntiles; }
+  __device__ TileInfo tile(int t) const {
+    const int4 e = tiles[t];
+    const GroupProblem p = probs[e.x];
+    return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x};
+  }
+};
+
+template <class F, class S>
+__global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_constant__ S sched, int* err) {
   extern __shared__ __align__(1024) char smem_raw[];
   char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + F::STAGES * F::STAGE);
@@ -195,10 +279,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_m = (M + F::BM - 1) / F::BM, tiles_n = (N + F::BN - 1) / F::BN;
-  const int tiles = tiles_m * tiles_n;
-  const int iters = (Kp / F::BK) * npair;           // stage iterations per tile
-  const int chunks = (iters + F::CH - 1) / F::CH;    // TMEM chunks per tile
+  const int tiles = sched.count();
 
   if(threadIdx.x == 0) {
     for(int s = 0; s < F::STAGES; ++s) {
@@ -225,24 +306,19 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     umma::regs_decrease<F::REGS_CTRL>();
     if(warp == 0 && lane == 0) {
       // ---------------------------------------------------------- producer
-      for(int p = 0; p < npair; ++p)
-        for(int t = 0; t < F::terms; ++t) {
-          tma_prefetch_desc(&maps.p[p].l[t]);
-          tma_prefetch_desc(&maps.p[p].r[t]);
-        }
       int g = 0;  // global stage iteration across tiles
       bool ok = true;
       for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-        int tile_m, tile_n;
-        tile_coords(tile, tiles_m, tiles_n, tile_m, tile_n);
-        const int m0 = tile_m * F::BM, n0 = tile_n * F::BN;
+        const TileInfo ti = sched.tile(tile);
+        const int m0 = ti.m0, n0 = ti.n0, npair = ti.npair;
+        const int iters = (ti.Kp / F::BK) * npair;
         for(int it = 0; it < iters; ++it, ++g) {
           const int s = g % F::STAGES;
           if(g >= F::STAGES && !mbar_wait(&empty[s], ((g / F::STAGES) - 1) & 1, err, kDevErrEmptyWait)) {
             ok = false;
             break;
           }
-          const ProductMaps& pm = maps.p[it % npair];
+          const ProductMaps& pm = ti.maps[it % npair];
           const int k0 = (it / npair) * F::BK;
           char* st = smem + s * F::STAGE;
           mbar_arrive_expect_tx(&full[s], F::STAGE);
@@ -261,6 +337,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       int g = 0, chunk = 0;
       bool ok = true;
       for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const TileInfo ti = sched.tile(tile);
+        const int iters = (ti.Kp / F::BK) * ti.npair;
         for(int it = 0; it < iters && ok; ++it, ++g) {
           const int b = chunk & 1;
           if(it % F::CH == 0) {
@@ -312,15 +390,18 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     umma::regs_increase<F::REGS_EPI>();
     const int q = warp & 3;          // TMEM lane quarter of this warp
     const int h = (warp - 4) >> 2;   // column half
-    const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
     float acc[F::HALF];
     int chunk = 0;
     bool ok = true;
     for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-      int tile_m, tile_n;
-      tile_coords(tile, tiles_m, tiles_n, tile_m, tile_n);
-      const int m = tile_m * F::BM + 32 * q + lane;
-      const int nbase = tile_n * F::BN + h * F::HALF;
+      const TileInfo ti = sched.tile(tile);
+      const int M = ti.M, N = ti.N;
+      const float alpha = ti.alpha, beta = ti.beta;
+      const int64_t ldc = ti.ldc;
+      const int chunks = ((ti.Kp / F::BK) * ti.npair + F::CH - 1) / F::CH;
+      const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(ti.C) & 15) == 0);
+      const int m = ti.m0 + 32 * q + lane;
+      const int nbase = ti.n0 + h * F::HALF;
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk & 1;
         if(!mbar_wait(&chunk_full[b], (chunk >> 1) & 1, err, kDevErrMmaWait)) {
@@ -342,7 +423,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         if(lane == 0) mbar_arrive(&chunk_empty[b]);
       }
       if(!ok || m >= M) continue;
-      float* crow = C + int64_t(m) * ldc + nbase;
+      float* crow = ti.C + int64_t(m) * ldc + nbase;
       if(vec && nbase + F::HALF <= N) {
 #pragma unroll
         for(int j = 0; j < F::HALF; j += 4) {
@@ -412,6 +493,30 @@ gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, i
   return GBPOLY_OK;
 }
 
+// Launch the tensor-core kernel for scheduler S: one persistent CTA per SM.
+template <class F, class S>
+gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t tiles, const char* kernel_name) {
+  static unsigned attr_set = 0;
+  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
+    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
+    // setmaxnreg redistributes the registers the CTA was launched with: the
+    // split must fit in threads x registers-per-thread at launch, or the
+    // increase would wait forever.
+    cudaFuncAttributes fa;
+    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F, S>));
+    const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
+    if(long(fa.numRegs) * F::THREADS < need)
+      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
+    attr_set |= 1u << ctx->device;
+  }
+  if(tiles <= 0) return GBPOLY_OK;
+  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
+  ProfileScope prof(ctx, kernel_name);
+  split_gemm_kernel<F, S><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(sched, ctx->err_dev);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
 // Workspace layout: terms x [A panel] then terms x [B panel] (B absent when
 // both operands are the same rows).
 struct Layout {
@@ -467,26 +572,9 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
     maps.p[1] = maps.p[0];
   }
 
-  static unsigned attr_set = 0;
-  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
-    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
-    // setmaxnreg redistributes the registers the CTA was launched with: the
-    // split must fit in threads x registers-per-thread at launch, or the
-    // increase would wait forever.
-    cudaFuncAttributes fa;
-    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F>));
-    const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
-    if(long(fa.numRegs) * F::THREADS < need)
-      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
-    attr_set |= 1u << ctx->device;
-  }
+  SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
   const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
-  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
-  ProfileScope prof(ctx, kernel_name);
-  split_gemm_kernel<F><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(maps, npair, int(a.M), int(a.N), int(Kp), a.alpha,
-      a.beta, a.C, a.ldc, ctx->err_dev);
-  GBPOLY_CUDA_TRY(cudaGetLastError());
-  return GBPOLY_OK;
+  return launch_tc_kernel<F>(ctx, sched, tiles, kernel_name);
 }
 
 template <class F>
@@ -539,6 +627,224 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
   return launch_gemm_tensor_config(ctx, prec, tuned_config(ctx, prec, a.M, a.N, a.K), a);
 }
+
+// ----------------------------------------------------------- grouped calls
+//
+// Many independent contractions of uneven shapes in two launches: one split
+// pass over all operands and one persistent tensor-core launch over the
+// tiles of all problems.  A plan prepares everything on the host once (term
+// panels, problem table, per-problem tensor maps, the tile list ordered by
+// decreasing K so that the round-robin walk of the persistent CTAs balances,
+// split jobs) and owns the device memory, so running it only enqueues the
+// two kernels and can be captured into a CUDA graph.
+
+}  // namespace gbpoly
+
+struct gbpoly_grouped {
+  gbpoly_precision prec;
+  std::vector<gbpoly_gemm_desc> descs;  // fp32: run as per-problem launches
+  void* dev = nullptr;                  // panels + tables
+  size_t dev_bytes = 0;
+  gbpoly::GroupProblem* probs = nullptr;
+  gbpoly::ProductMaps* maps = nullptr;
+  int4* tiles = nullptr;
+  gbpoly::SplitJob* jobs = nullptr;
+  int ntiles = 0, njobs = 0, split_blocks = 0;
+  int64_t flops = 0;
+};
+
+namespace gbpoly {
+namespace {
+
+template <class F>
+gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
+  const int P = int(g->descs.size());
+  // layout: panels first, then problem table, tensor maps, tiles, jobs
+  std::vector<size_t> a_off(P), b_off(P);
+  std::vector<int64_t> kp(P);
+  size_t off = 0;
+  for(int i = 0; i < P; ++i) {
+    const auto& d = g->descs[i];
+    kp[i] = int64_t(align_up(size_t(std::max<int64_t>(d.K, 1)), 64));
+    a_off[i] = off;
+    off += F::terms * align_up(size_t(d.M) * kp[i] * F::esz, 1024);
+    b_off[i] = off;
+    off += F::terms * align_up(size_t(d.N) * kp[i] * F::esz, 1024);
+  }
+  const size_t probs_off = align_up(off, 256), maps_off = align_up(probs_off + P * sizeof(GroupProblem), 128);
+  std::vector<int4> tiles;
+  for(int i = 0; i < P; ++i) {
+    const auto& d = g->descs[i];
+    const int tm = int((d.M + F::BM - 1) / F::BM), tn = int((d.N + F::BN - 1) / F::BN);
+    for(int x = 0; x < tm; ++x)
+      for(int y = 0; y < tn; ++y) tiles.push_back(make_int4(i, x, y, 0));
+  }
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const int4& u, const int4& v) { return kp[u.x] > kp[v.x]; });
+  const size_t tiles_off = align_up(maps_off + P * sizeof(ProductMaps), 256);
+  const size_t jobs_off = align_up(tiles_off + tiles.size() * sizeof(int4), 256);
+  const size_t total = jobs_off + 2 * P * sizeof(SplitJob);
+  GBPOLY_CUDA_TRY(cudaMalloc(&g->dev, total));
+  g->dev_bytes = total;
+  char* base = static_cast<char*>(g->dev);
+
+  std::vector<GroupProblem> probs(P);
+  std::vector<ProductMaps> maps(P);
+  std::vector<SplitJob> jobs;
+  int blocks = 0;
+  gbpoly_status st;
+  for(int i = 0; i < P; ++i) {
+    const auto& d = g->descs[i];
+    probs[i] = GroupProblem{int(d.M), int(d.N), int(kp[i]), 0, d.alpha, d.beta, d.C, d.ldc};
+    const size_t sa = align_up(size_t(d.M) * kp[i] * F::esz, 1024), sb = align_up(size_t(d.N) * kp[i] * F::esz, 1024);
+    Panels pa{base + a_off[i], sa}, pb{base + b_off[i], sb};
+    if(d.M > 0 && d.N > 0) {
+      if((st = make_product_maps<F>(ctx, maps[i], pa, d.M, pb, d.N, kp[i])) != GBPOLY_OK) return st;
+      const int kb = int(kp[i] / 64);
+      jobs.push_back(SplitJob{d.A, d.lda, d.op_a == GBPOLY_OP_N ? 1 : 0, int(d.M), int(d.K), int(kp[i]), pa.base,
+          int64_t(sa / F::esz), blocks, kb});
+      blocks += int((d.M + 63) / 64) * kb;
+      jobs.push_back(SplitJob{d.B, d.ldb, d.op_b == GBPOLY_OP_T ? 1 : 0, int(d.N), int(d.K), int(kp[i]), pb.base,
+          int64_t(sb / F::esz), blocks, kb});
+      blocks += int((d.N + 63) / 64) * kb;
+    }
+    g->flops += 2 * d.M * d.N * d.K;
+  }
+  g->probs = reinterpret_cast<GroupProblem*>(base + probs_off);
+  g->maps = reinterpret_cast<ProductMaps*>(base + maps_off);
+  g->tiles = reinterpret_cast<int4*>(base + tiles_off);
+  g->jobs = reinterpret_cast<SplitJob*>(base + jobs_off);
+  g->ntiles = int(tiles.size());
+  g->njobs = int(jobs.size());
+  g->split_blocks = blocks;
+  GBPOLY_CUDA_TRY(cudaMemcpy(g->probs, probs.data(), P * sizeof(GroupProblem), cudaMemcpyHostToDevice));
+  GBPOLY_CUDA_TRY(cudaMemcpy(g->maps, maps.data(), P * sizeof(ProductMaps), cudaMemcpyHostToDevice));
+  if(!tiles.empty())
+    GBPOLY_CUDA_TRY(cudaMemcpy(g->tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  if(!jobs.empty())
+    GBPOLY_CUDA_TRY(cudaMemcpy(g->jobs, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice));
+  return GBPOLY_OK;
+}
+
+template <class F>
+gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) {
+  using T = typename Term<F::elem>::T;
+  if(g->split_blocks > 0) {
+    ProfileScope prof(ctx, "grouped_split");
+    grouped_split_kernel<F::elem, F::terms><<<g->split_blocks, 256, 0, ctx->stream>>>(g->jobs, g->njobs);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+  }
+  (void)sizeof(T);
+  GroupedSched<F::BM, F::BN> sched{g->probs, g->maps, g->tiles, g->ntiles};
+  return launch_tc_kernel<F>(ctx, sched, g->ntiles, name);
+}
+
+// Grouped calls use the 128-column tile configurations (less padding on small problems).
+using GroupBF16x3 = FormBF16x3_c;
+using GroupTF32x3 = FormTF32x3_c;
+using GroupBF16x6 = FormBF16x6_b;
+using GroupTF32 = FormTF32_c;
+
+}  // namespace
+}  // namespace gbpoly
+
+extern "C" {
+
+gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
+    gbpoly_grouped** out) {
+  using namespace gbpoly;
+  if(!ctx || !out || count < 0 || (count > 0 && !descs)) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  *out = nullptr;
+  GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
+  for(int i = 0; i < count; ++i) {
+    const auto& d = descs[i];
+    const bool bad_op = (d.op_a != GBPOLY_OP_N && d.op_a != GBPOLY_OP_T) || (d.op_b != GBPOLY_OP_N && d.op_b != GBPOLY_OP_T);
+    const int64_t ac = d.op_a == GBPOLY_OP_N ? d.K : d.M, ar = d.op_a == GBPOLY_OP_N ? d.M : d.K;
+    const int64_t bc = d.op_b == GBPOLY_OP_N ? d.N : d.K, br = d.op_b == GBPOLY_OP_N ? d.K : d.N;
+    if(bad_op || d.M < 0 || d.N < 0 || d.K < 0 || d.M >= (1ll << 31) || d.N >= (1ll << 31) || d.K >= (1ll << 30) ||
+        (ar > 0 && ac > 0 && (!d.A || d.lda < ac)) || (br > 0 && bc > 0 && (!d.B || d.ldb < bc)) ||
+        (d.M > 0 && d.N > 0 && (!d.C || d.ldc < d.N))) {
+      char buf[96];
+      snprintf(buf, sizeof buf, "grouped problem %d: bad shape, operation, pointer or leading dimension", i);
+      return fail(GBPOLY_ERR_INVALID, buf);
+    }
+  }
+  auto* g = new gbpoly_grouped();
+  g->prec = prec;
+  g->descs.assign(descs, descs + count);
+  gbpoly_status st = GBPOLY_OK;
+  switch(prec) {
+  case GBPOLY_PREC_FP32:
+    for(auto& d : g->descs) g->flops += 2 * d.M * d.N * d.K;
+    break;
+  case GBPOLY_PREC_BF16X3: st = plan_grouped<GroupBF16x3>(ctx, g); break;
+  case GBPOLY_PREC_TF32X3: st = plan_grouped<GroupTF32x3>(ctx, g); break;
+  case GBPOLY_PREC_BF16X6: st = plan_grouped<GroupBF16x6>(ctx, g); break;
+  case GBPOLY_PREC_TF32: st = plan_grouped<GroupTF32>(ctx, g); break;
+  default: st = fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
+  }
+  if(st != GBPOLY_OK) {
+    if(g->dev) cudaFree(g->dev);
+    delete g;
+    return st;
+  }
+  *out = g;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
+  using namespace gbpoly;
+  if(!ctx || !g) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
+  switch(g->prec) {
+  case GBPOLY_PREC_FP32:
+    for(const auto& d : g->descs) {
+      GemmF32Args a{};
+      a.M = d.M, a.N = d.N, a.K = d.K, a.alpha = d.alpha, a.beta = d.beta, a.op_a = d.op_a, a.op_b = d.op_b;
+      a.A = d.A, a.lda = d.lda, a.B = d.B, a.ldb = d.ldb, a.C = d.C, a.ldc = d.ldc;
+      gbpoly_status st = launch_gemm_f32_simt(ctx, a);
+      if(st != GBPOLY_OK) return st;
+    }
+    return GBPOLY_OK;
+  case GBPOLY_PREC_BF16X3: return run_grouped<GroupBF16x3>(ctx, g, "grouped_bf16x3_gemm");
+  case GBPOLY_PREC_TF32X3: return run_grouped<GroupTF32x3>(ctx, g, "grouped_tf32x3_gemm");
+  case GBPOLY_PREC_BF16X6: return run_grouped<GroupBF16x6>(ctx, g, "grouped_bf16x6_gemm");
+  case GBPOLY_PREC_TF32: return run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
+  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
+  }
+}
+
+gbpoly_status gbpoly_grouped_info(gbpoly_grouped* g, int64_t* flops, int* tiles, size_t* device_bytes) {
+  if(!g) return gbpoly::fail(GBPOLY_ERR_INVALID, "null plan");
+  if(flops) *flops = g->flops;
+  if(tiles) *tiles = g->ntiles;
+  if(device_bytes) *device_bytes = g->dev_bytes;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_grouped_destroy(gbpoly_ctx* ctx, gbpoly_grouped* g) {
+  if(!g) return GBPOLY_OK;
+  if(ctx) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  if(g->dev) cudaFree(g->dev);
+  delete g;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_gemm_grouped_f32(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count) {
+  gbpoly_grouped* g = nullptr;
+  gbpoly_status st = gbpoly_grouped_plan(ctx, prec, descs, count, &g);
+  if(st != GBPOLY_OK) return st;
+  st = gbpoly_grouped_run(ctx, g);
+  gbpoly_status st2 = gbpoly_grouped_destroy(ctx, g);  // waits for the launches
+  return st != GBPOLY_OK ? st : st2;
+}
+
+}  // extern "C"
+
+namespace gbpoly {
 
 // ------------------------------------------------ allocation-free entry point
 //
@@ -608,22 +914,9 @@ gbpoly_status launch_gemm_bf16x3_noalloc(gbpoly_ctx* ctx, const GemmF32Args& a) 
   GemmMaps maps;
   if((st = make_product_maps<F>(ctx, maps.p[0], pa, a.M, pb, a.N, lay.Kp)) != GBPOLY_OK) return st;
   maps.p[1] = maps.p[0];
-  static unsigned attr_set = 0;
-  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
-    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
-    cudaFuncAttributes fa;
-    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F>));
-    if(long(fa.numRegs) * F::THREADS < 128l * F::REGS_CTRL + 256l * F::REGS_EPI)
-      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
-    attr_set |= 1u << ctx->device;
-  }
+  SingleSched<F::BM, F::BN> sched{maps, 1, int(a.M), int(a.N), int(lay.Kp), a.alpha, a.beta, a.C, a.ldc};
   const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
-  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
-  ProfileScope prof(ctx, "bf16x3_gemm_noalloc");
-  split_gemm_kernel<F><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(maps, 1, int(a.M), int(a.N), int(lay.Kp), a.alpha,
-      a.beta, a.C, a.ldc, ctx->err_dev);
-  GBPOLY_CUDA_TRY(cudaGetLastError());
-  return GBPOLY_OK;
+  return launch_tc_kernel<F>(ctx, sched, tiles, "bf16x3_gemm_noalloc");
 }
 
 }  // namespace gbpoly

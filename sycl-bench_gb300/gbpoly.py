@@ -56,6 +56,13 @@ class Op(enum.IntEnum):
 _c_i64 = ct.c_int64
 _vp = ct.c_void_p
 
+
+class GemmDesc(ct.Structure):
+    """gbpoly_gemm_desc: C = alpha * op(A) op(B) + beta * C."""
+    _fields_ = [("op_a", ct.c_int), ("op_b", ct.c_int), ("M", ct.c_int64), ("N", ct.c_int64), ("K", ct.c_int64),
+                ("alpha", ct.c_float), ("beta", ct.c_float), ("A", ct.c_void_p), ("lda", ct.c_int64),
+                ("B", ct.c_void_p), ("ldb", ct.c_int64), ("C", ct.c_void_p), ("ldc", ct.c_int64)]
+
 # name -> (restype, argtypes); every exported symbol of include/gbpoly.h
 SIGNATURES: dict[str, tuple] = {
     "gbpoly_init": (ct.c_int, [ct.c_int, ct.POINTER(_vp)]),
@@ -99,6 +106,11 @@ SIGNATURES: dict[str, tuple] = {
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
                                     ct.c_float, _vp, _c_i64]),
+    "gbpoly_grouped_plan": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.POINTER(_vp)]),
+    "gbpoly_grouped_run": (ct.c_int, [_vp, _vp]),
+    "gbpoly_grouped_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int), ct.POINTER(ct.c_size_t)]),
+    "gbpoly_grouped_destroy": (ct.c_int, [_vp, _vp]),
+    "gbpoly_gemm_grouped_f32": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int]),
     "gbpoly_gemm_f32_bf16x3_noalloc": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
                                                   _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_gemm_f64": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, _vp,
@@ -312,6 +324,36 @@ class Context:
         n = ct.c_int()
         _check(self.lib.gbpoly_autotune_load(self.handle, str(path).encode(), ct.byref(n)))
         return n.value
+
+    # -- grouped contractions
+    @staticmethod
+    def descs(items) -> ct.Array:
+        """items: dicts with M, N, K, alpha, beta, A, lda, B, ldb, C, ldc[, op_a, op_b] (device buffers or ints)."""
+        arr = (GemmDesc * len(items))()
+        for d, it in zip(arr, items):
+            d.op_a, d.op_b = int(it.get("op_a", Op.N)), int(it.get("op_b", Op.N))
+            d.M, d.N, d.K = it["M"], it["N"], it["K"]
+            d.alpha, d.beta = it["alpha"], it["beta"]
+            d.A, d.lda = int(it["A"]) or None, it["lda"]
+            d.B, d.ldb = int(it["B"]) or None, it["ldb"]
+            d.C, d.ldc = int(it["C"]) or None, it["ldc"]
+        return arr
+
+    def grouped_plan(self, prec, descs):
+        h = _vp()
+        _check(self.lib.gbpoly_grouped_plan(self.handle, int(prec), ct.cast(descs, _vp), len(descs), ct.byref(h)))
+        return h
+
+    def grouped_run(self, plan) -> None:
+        _check(self.lib.gbpoly_grouped_run(self.handle, plan))
+
+    def grouped_info(self, plan) -> dict:
+        f, t, b = ct.c_int64(), ct.c_int(), ct.c_size_t()
+        _check(self.lib.gbpoly_grouped_info(plan, ct.byref(f), ct.byref(t), ct.byref(b)))
+        return {"flops": f.value, "tiles": t.value, "device_bytes": b.value}
+
+    def grouped_destroy(self, plan) -> None:
+        _check(self.lib.gbpoly_grouped_destroy(self.handle, plan))
 
     def graph_begin(self) -> None:
         _check(self.lib.gbpoly_graph_begin(self.handle))

@@ -1,0 +1,101 @@
+"""Grouped contractions (one split pass + one persistent tensor-core launch
+over all problems) against the FP64 oracle, problem by problem.
+
+Workload shape of the grouped benchmark: M, N, K log-uniform, entries
+uniform[-1, 1] times a per-matrix scale log-uniform in [1e-3, 1e3],
+C = A.B + 0.5 C; here with smaller sizes so the oracle finishes quickly,
+plus degenerate problems (K = 0, 1 x 1, transposed operands)."""
+import numpy as np
+import pytest
+
+import gbpoly
+import oracle
+from gbpoly import Op, Precision
+
+pytestmark = pytest.mark.gpu
+
+BOUND = {Precision.FP32: 2e-5, Precision.TF32: 2e-3, Precision.BF16X3: 3e-5, Precision.TF32X3: 5e-6,
+         Precision.BF16X6: 5e-6}
+
+
+def make_problems(rng, count, lo, hi):
+    probs = []
+    for i in range(count):
+        M, N, K = (int(np.exp(rng.uniform(np.log(lo), np.log(hi)))) for _ in range(3))
+        op_a = Op.T if i % 5 == 3 else Op.N
+        op_b = Op.T if i % 3 == 1 else Op.N
+        scale = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e3))))
+        A = (rng.uniform(-1, 1, (K, M) if op_a == Op.T else (M, K)) * scale).astype(np.float32)
+        B = rng.uniform(-1, 1, (N, K) if op_b == Op.T else (K, N)).astype(np.float32)
+        C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+        probs.append((op_a, op_b, M, N, K, A, B, C))
+    probs.append((Op.N, Op.N, 70, 90, 0, np.zeros((70, 0), np.float32), np.zeros((0, 90), np.float32),
+                  rng.uniform(-1, 1, (70, 90)).astype(np.float32)))  # K = 0: C = 0.5 C
+    probs.append((Op.N, Op.N, 1, 1, 1, np.full((1, 1), 3, np.float32), np.full((1, 1), 5, np.float32),
+                  np.ones((1, 1), np.float32)))
+    return probs
+
+
+def run_group(ctx, prec, probs):
+    items, bufs = [], []
+    for op_a, op_b, M, N, K, A, B, C in probs:
+        dA = ctx.upload(A) if A.size else ctx.alloc(16)
+        dB = ctx.upload(B) if B.size else ctx.alloc(16)
+        dC = ctx.upload(C)
+        bufs.append((dA, dB, dC))
+        items.append(dict(op_a=op_a, op_b=op_b, M=M, N=N, K=K, alpha=1.0, beta=0.5, A=dA, lda=max(A.shape[1], 1),
+                          B=dB, ldb=max(B.shape[1], 1), C=dC, ldc=N))
+    descs = ctx.descs(items)
+    plan = ctx.grouped_plan(prec, descs)
+    return plan, bufs
+
+
+@pytest.mark.parametrize("prec", list(BOUND))
+def test_grouped_matches_fp64_per_problem(ctx, prec):
+    rng = np.random.default_rng(21)
+    probs = make_problems(rng, 40, 16, 700)
+    plan, bufs = run_group(ctx, prec, probs)
+    info = ctx.grouped_info(plan)
+    assert info["flops"] == sum(2 * p[2] * p[3] * p[4] for p in probs)
+    ctx.grouped_run(plan)
+    ctx.synchronize()
+    for (op_a, op_b, M, N, K, A, B, C), (_, _, dC) in zip(probs, bufs):
+        out = ctx.download(dC, (M, N))
+        if K == 0:
+            np.testing.assert_allclose(out, 0.5 * C, rtol=1e-7)
+            continue
+        ref = oracle.gemm_f64(A, B, C, 1.0, 0.5, op_a=int(op_a), op_b=int(op_b))
+        frob = oracle.error_norms(out, ref)[1]
+        assert frob < BOUND[prec], (prec.name, M, N, K, frob)
+    ctx.grouped_destroy(plan)
+    for b in bufs:
+        for x in b:
+            ctx.free(x)
+
+
+def test_grouped_run_in_a_graph(ctx):
+    rng = np.random.default_rng(5)
+    probs = make_problems(rng, 12, 64, 400)
+    plan, bufs = run_group(ctx, Precision.BF16X3, probs)
+    ctx.grouped_run(plan)
+    ctx.synchronize()
+    eager = [ctx.download(b[2], (p[2], p[3])) for p, b in zip(probs, bufs)]
+    ctx.graph_begin()
+    ctx.grouped_run(plan)
+    g = ctx.graph_end()
+    for p, b in zip(probs, bufs):
+        ctx.h2d(b[2], p[7])  # restore C (beta = 0.5 reads it)
+    ctx.graph_launch(g)
+    ctx.synchronize()
+    for e, p, b in zip(eager, probs, bufs):
+        np.testing.assert_array_equal(ctx.download(b[2], (p[2], p[3])), e)
+    ctx.graph_destroy(g)
+    ctx.grouped_destroy(plan)
+
+
+def test_grouped_rejects_bad_descriptor(ctx):
+    d = ctx.alloc(64)
+    descs = ctx.descs([dict(M=4, N=4, K=4, alpha=1.0, beta=0.0, A=d, lda=2, B=d, ldb=4, C=d, ldc=4)])
+    with pytest.raises(gbpoly.GbpolyError) as e:
+        ctx.grouped_plan(Precision.BF16X3, descs)
+    assert e.value.status == gbpoly.Status.INVALID and b"problem 0" in ctx.lib.gbpoly_last_error()
