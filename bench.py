@@ -378,8 +378,17 @@ def run_grouped_workload(ctx, args) -> dict:
         e1.record()
         ctx.synchronize()
         ms = e0.elapsed_ms(e1) / args.steps
+        # one more eager run with per-kernel events: where the step's time goes
+        ctx.profile_read()
+        ctx.profile(True)
+        ctx.grouped_run(plan)
+        ctx.synchronize()
+        ctx.profile(False)
+        kern = {k: round(t / c, 4) for k, (c, t) in ctx.profile_read().items()}
         out[prec.name.lower()] = {"mode": mode, "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12, **err,
-                                  "launches_per_step": 1 if graph is not None else count}
+                                  "launches_per_step": 2 if graph is not None else count,
+                                  "kernel_ms_eager": kern if graph is not None else
+                                  {"sgemm (all launches)": round(sum(kern.values()), 4)}}
         if graph is not None:
             ctx.graph_destroy(graph)
         ctx.grouped_destroy(plan)
