@@ -61,7 +61,8 @@ struct Form {
   static constexpr int KMMA = E == Elem::BF16 ? 16 : 8;  // K of one tcgen05.mma (32 bytes)
   static constexpr int A_TILE = BM * ROW, B_TILE = BN * ROW;
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int EPI_STAGE = 8 * 32 * 33 * 4;  // epilogue staging, one 32x33 fp32 tile per warp
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + EPI_STAGE;
   // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
   // accumulation inside the tensor core stays short); chunks are summed in
   // FP32 registers, round to nearest, by the epilogue warps.  Two chunk
@@ -89,7 +90,7 @@ using FormTF32x3_b = Form<Elem::TF32, 2, 3, 256, 4, 64>;
 using FormTF32x3_c = Form<Elem::TF32, 2, 3, 128, 3>;
 using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
 using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
-using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 3, 64>;
+using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 2, 64>;
 
 // Term indices of product p: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 ? 1 : (p == 4 ? 1 : (p == 5 ? 2 : 0)); }
@@ -129,15 +130,39 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ X, int64_t 
     typename Term<E>::T* __restrict__ out, int64_t panel_stride, int64_t r0, int64_t k0, float (*tile)[65]) {
   using T = typename Term<E>::T;
   const int tid = threadIdx.x;
+  // Load the 64 x 64 block of op(X) into shared memory, coalesced along X's
+  // contiguous dimension; 128-bit loads when the block is whole and aligned.
+  const int64_t r_lim = R - r0, k_lim = K - k0;
+  const bool whole = r_lim >= 64 && k_lim >= 64 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  if(whole) {
 #pragma unroll
-  for(int e = 0; e < 16; ++e) {
-    const int idx = tid + e * 256;
-    const int rr = k_major ? (idx >> 6) : (idx & 63);
-    const int kk = k_major ? (idx & 63) : (idx >> 6);
-    const int64_t r = r0 + rr, k = k0 + kk;
-    float v = 0.f;
-    if(r < R && k < K) v = k_major ? X[r * ld + k] : X[k * ld + r];
-    tile[rr][kk] = v;
+    for(int e = 0; e < 4; ++e) {
+      const int idx = tid + e * 256;          // 0..1023 float4 of the block
+      const int outer = idx >> 4, inner = (idx & 15) * 4;
+      if(k_major) {  // rows of X are rows of op(X): read along k
+        const float4 v = *reinterpret_cast<const float4*>(X + (r0 + outer) * ld + k0 + inner);
+        tile[outer][inner] = v.x;
+        tile[outer][inner + 1] = v.y;
+        tile[outer][inner + 2] = v.z;
+        tile[outer][inner + 3] = v.w;
+      } else {  // rows of X are k: read along r
+        const float4 v = *reinterpret_cast<const float4*>(X + (k0 + outer) * ld + r0 + inner);
+        tile[inner][outer] = v.x;
+        tile[inner + 1][outer] = v.y;
+        tile[inner + 2][outer] = v.z;
+        tile[inner + 3][outer] = v.w;
+      }
+    }
+  } else {
+#pragma unroll
+    for(int e = 0; e < 16; ++e) {
+      const int idx = tid + e * 256;
+      const int rr = k_major ? (idx >> 6) : (idx & 63);
+      const int kk = k_major ? (idx & 63) : (idx >> 6);
+      float v = 0.f;
+      if(rr < r_lim && kk < k_lim) v = k_major ? X[(r0 + rr) * ld + k0 + kk] : X[(k0 + kk) * ld + r0 + rr];
+      tile[rr][kk] = v;
+    }
   }
   __syncthreads();
   const int rr = tid >> 2, kc = (tid & 3) * 16;
@@ -277,6 +302,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   uint64_t* chunk_empty = chunk_full + 2;    // [2]
   uint64_t* drain = chunk_empty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  float(*epi_stage)[33] = reinterpret_cast<float(*)[33]>(smem + F::STAGES * F::STAGE + 256);  // 8 warps x [32][33]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = sched.count();
@@ -399,8 +425,6 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       const float alpha = ti.alpha, beta = ti.beta;
       const int64_t ldc = ti.ldc;
       const int chunks = ((ti.Kp / F::BK) * ti.npair + F::CH - 1) / F::CH;
-      const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(ti.C) & 15) == 0);
-      const int m = ti.m0 + 32 * q + lane;
       const int nbase = ti.n0 + h * F::HALF;
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk & 1;
@@ -422,29 +446,29 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         __syncwarp();
         if(lane == 0) mbar_arrive(&chunk_empty[b]);
       }
-      if(!ok || m >= M) continue;
-      float* crow = ti.C + int64_t(m) * ldc + nbase;
-      if(vec && nbase + F::HALF <= N) {
+      if(!ok) continue;
+      // Write C through a per-warp 32 x 32 staging tile: each lane holds one
+      // row of the block, the stores go out one 128-byte row segment per
+      // instruction (coalesced for any ldc and alignment).
+      float(*stage)[33] = epi_stage + (warp - 4) * 32;
+      const int row0 = ti.m0 + 32 * q;
 #pragma unroll
-        for(int j = 0; j < F::HALF; j += 4) {
-          float4 o = make_float4(alpha * acc[j], alpha * acc[j + 1], alpha * acc[j + 2], alpha * acc[j + 3]);
-          if(beta != 0.f) {
-            const float4 cv = *reinterpret_cast<const float4*>(crow + j);
-            o.x = fmaf(beta, cv.x, o.x);
-            o.y = fmaf(beta, cv.y, o.y);
-            o.z = fmaf(beta, cv.z, o.z);
-            o.w = fmaf(beta, cv.w, o.w);
-          }
-          *reinterpret_cast<float4*>(crow + j) = o;
-        }
-      } else {
+      for(int j = 0; j < F::HALF / 32; ++j) {
 #pragma unroll
-        for(int j = 0; j < F::HALF; ++j) {
-          if(nbase + j < N) {
-            const float v = alpha * acc[j];
-            crow[j] = (beta != 0.f) ? fmaf(beta, crow[j], v) : v;
-          }
+        for(int i = 0; i < 32; ++i) stage[lane][i] = acc[32 * j + i];
+        __syncwarp();
+        const int n = nbase + 32 * j + lane;
+        if(n < N) {
+          const int rows = min(32, M - row0);
+          float* col = ti.C + int64_t(row0) * ldc + n;
+          float cv[32];  // all 32 loads in flight before the first store
+#pragma unroll
+          for(int r = 0; r < 32; ++r) cv[r] = (beta != 0.f && r < rows) ? col[int64_t(r) * ldc] : 0.f;
+#pragma unroll
+          for(int r = 0; r < 32; ++r)
+            if(r < rows) col[int64_t(r) * ldc] = fmaf(beta, cv[r], alpha * stage[r][lane]);
         }
+        __syncwarp();
       }
     }
   }
