@@ -183,7 +183,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     def fresh_c():
         ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(dC), gbpoly._ptr(dC0), nbytes)
 
-    forms = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.TF32]
+    forms = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.TF32, Precision.FP8]
     headline = Precision.BF16X3
     tiers = {}
     sampler = ClockSampler(dist.local_rank)
@@ -282,7 +282,8 @@ def run_gpu(args, dist: Dist) -> dict | None:
     else:
         # BF16-MMA equivalents per algorithmic multiply-add (a TF32 MMA runs at half the BF16 rate):
         # bf16x3 3, tf32x3 and bf16x6 6, tf32 2.  The form's ceiling is the BF16 peak divided by that.
-        mma_per_mac = {Precision.BF16X3: 3, Precision.TF32X3: 6, Precision.BF16X6: 6, Precision.TF32: 2}[headline]
+        mma_per_mac = {Precision.BF16X3: 3, Precision.TF32X3: 6, Precision.BF16X6: 6, Precision.TF32: 2,
+                       Precision.FP8: 0.5}[headline]
         bf16 = peaks["bf16_tflops"]
         peak = bf16 / mma_per_mac
         roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",

@@ -9,6 +9,7 @@
 //   bf16x3    BF16  2      a0.b0 + a0.b1 + a1.b0                 ~16
 //   tf32x3    TF32  2      a0.b0 + a0.b1 + a1.b0                 ~22-24
 //   bf16x6    BF16  3      a0.b0 + a0.b1 + a1.b0 + a0.b2 + a1.b1 + a2.b0   ~24
+//   fp8       E4M3  1      a0.b0, each operand with one scale per 128x128 block   4
 // Two kernels per call:
 //   * split_kernel (memory bound): writes the K-major term panels of an
 //     operand into the context workspace (transposing through shared memory
@@ -37,6 +38,7 @@
 //     into the same accumulator.
 // All mbarrier waits are bounded (gbpoly_internal.cuh).
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <stdio.h>
 
 #include <algorithm>
@@ -49,16 +51,19 @@
 namespace gbpoly {
 namespace {
 
-enum class Elem { BF16, TF32 };
+enum class Elem { BF16, TF32, E4M3 };
 
 template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128>
 struct Form {
   static constexpr Elem elem = E;
   static constexpr int terms = TERMS, nprod = NPROD, BM = 128, BN = BN_, STAGES = STAGES_;
   static constexpr int ROW = ROW_;                       // bytes of K per smem row (= swizzle width)
-  static constexpr int esz = E == Elem::BF16 ? 2 : 4;
+  static constexpr int esz = E == Elem::BF16 ? 2 : (E == Elem::TF32 ? 4 : 1);
   static constexpr int BK = ROW / esz;                   // K elements per stage
-  static constexpr int KMMA = E == Elem::BF16 ? 16 : 8;  // K of one tcgen05.mma (32 bytes)
+  static constexpr int KMMA = 32 / esz;                  // K of one tcgen05.mma (32 bytes)
+  // E4M3 operands carry one scale per 128 x 128 block: a stage (128 bytes of
+  // K) is exactly one block along K, so each TMEM chunk has one scale.
+  static constexpr bool scaled = E == Elem::E4M3;
   static constexpr int A_TILE = BM * ROW, B_TILE = BN * ROW;
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);
   static constexpr int EPI_STAGE = 8 * 32 * 33 * 4;  // epilogue staging, one 32x33 fp32 tile per warp
@@ -73,7 +78,9 @@ struct Form {
   static constexpr int THREADS = 384;  // warpgroup 0: producer, MMA; warpgroups 1-2: epilogue
   static constexpr uint32_t REGS_CTRL = 56, REGS_EPI = 208;
   static constexpr uint32_t IDESC =
-      umma::InstrDesc<BM, BN, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
+      E == Elem::E4M3 ? umma::InstrDescE4M3<BM, BN>::value
+                      : umma::InstrDesc<BM, BN, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
+  static_assert(!scaled || (ROW == 128 && CH == 1), "one scale block per chunk");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert(TMEM_COLS <= 512, "tensor memory");
 };
@@ -91,6 +98,7 @@ using FormTF32x3_c = Form<Elem::TF32, 2, 3, 128, 3>;
 using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
 using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
 using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 2, 64>;
+using FormFP8 = Form<Elem::E4M3, 1, 1, 128, 6>;
 
 // Term indices of product p: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 ? 1 : (p == 4 ? 1 : (p == 5 ? 2 : 0)); }
@@ -224,6 +232,50 @@ __global__ void __launch_bounds__(256) grouped_split_kernel(const SplitJob* __re
       j.panel_stride, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, tile);
 }
 
+// ---------------------------------------------------------- FP8 quantize --
+// One 128 x 128 block of op(X) (rows x K, zero beyond R and K) per CTA:
+// scale = max|x| / 448 (1 for an all-zero block), q = e4m3(x / scale) with
+// saturation, written K-major into out[R][Kp]; scale into
+// scales[row block][Kp / 128].
+__global__ void __launch_bounds__(256) quantize_e4m3_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R,
+    int K, int Kp, uint8_t* __restrict__ out, float* __restrict__ scales) {
+  extern __shared__ float blk[];  // [128][129]
+  __shared__ float red[8];
+  const int tid = threadIdx.x;
+  const int64_t r0 = int64_t(blockIdx.y) * 128, k0 = int64_t(blockIdx.x) * 128;
+  float amax = 0.f;
+  for(int e = 0; e < 64; ++e) {
+    const int idx = tid + e * 256;  // 0..16383
+    const int rr = k_major ? (idx >> 7) : (idx & 127);
+    const int kk = k_major ? (idx & 127) : (idx >> 7);
+    const int64_t r = r0 + rr, k = k0 + kk;
+    float v = 0.f;
+    if(r < R && k < K) v = k_major ? X[r * ld + k] : X[k * ld + r];
+    blk[rr * 129 + kk] = v;
+    amax = fmaxf(amax, fabsf(v));
+  }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if((tid & 31) == 0) red[tid >> 5] = amax;
+  __syncthreads();
+  float m = red[0];
+#pragma unroll
+  for(int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+  const float scale = m > 0.f ? m / 448.f : 1.f;
+  const float inv = 1.f / scale;
+  if(tid == 0) scales[int64_t(blockIdx.y) * (Kp / 128) + blockIdx.x] = scale;
+  // each thread: one row, 64 consecutive k (two threads per row)
+  const int rr = tid >> 1, kc = (tid & 1) * 64;
+  const int64_t r = r0 + rr;
+  if(r >= R) return;
+  __align__(16) __nv_fp8_storage_t q[64];
+#pragma unroll
+  for(int i = 0; i < 64; ++i) q[i] = __nv_cvt_float_to_fp8(blk[rr * 129 + kc + i] * inv, __NV_SATFINITE, __NV_E4M3);
+  uint4* dst = reinterpret_cast<uint4*>(out + r * Kp + k0 + kc);
+#pragma unroll
+  for(int v = 0; v < 4; ++v) dst[v] = reinterpret_cast<const uint4*>(q)[v];
+}
+
 // Tensor maps of one product pairing: left operand terms in 128-row boxes,
 // right operand terms in BN-row boxes.
 struct ProductMaps {
@@ -251,6 +303,11 @@ struct TileInfo {
   float* C;
   int64_t ldc;
   const ProductMaps* maps;  // [npair]
+  // E4M3 only: per pairing, scales of the left and right operand blocks,
+  // [row block][k block] with kt k blocks per row block
+  const float* sl[2];
+  const float* sr[2];
+  int kt;
 };
 
 // One contraction: tiles in grouped raster order, tensor maps in the
@@ -262,11 +319,14 @@ struct SingleSched {
   float alpha, beta;
   float* C;
   int64_t ldc;
+  const float* sl[2] = {nullptr, nullptr};
+  const float* sr[2] = {nullptr, nullptr};
   __device__ int count() const { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
   __device__ TileInfo tile(int t) const {
     int tm, tn;
     tile_coords(t, (M + BM - 1) / BM, (N + BN - 1) / BN, tm, tn);
-    return TileInfo{tm * BM, tn * BN, M, N, Kp, npair, alpha, beta, C, ldc, maps.p};
+    return TileInfo{tm * BM, tn * BN, M, N, Kp, npair, alpha, beta, C, ldc, maps.p, {sl[0], sl[1]}, {sr[0], sr[1]},
+        Kp / 128};
   }
 };
 
@@ -288,7 +348,8 @@ struct GroupedSched {
   __device__ TileInfo tile(int t) const {
     const int4 e = tiles[t];
     const GroupProblem p = probs[e.x];
-    return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x};
+    return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x,
+        {nullptr, nullptr}, {nullptr, nullptr}, 0};
   }
 };
 
@@ -398,8 +459,10 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             const uint32_t acc = (it % F::CH != 0 || q > 0) ? 1u : 0u;
             if constexpr(F::elem == Elem::BF16)
               umma::mma_f16(d, da, db, F::IDESC, acc);
-            else
+            else if constexpr(F::elem == Elem::TF32)
               umma::mma_tf32(d, da, db, F::IDESC, acc);
+            else
+              umma::mma_f8(d, da, db, F::IDESC, acc);
           }
           umma::commit(&empty[s]);  // stage s is free once these MMAs have read it
           if(it % F::CH == F::CH - 1 || it == iters - 1) {
@@ -434,13 +497,23 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
         umma::fence_after_sync();
         const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b * F::BN + h * F::HALF);
+        float sc = 1.f;  // block scale of this chunk (E4M3): left row block x right column block
+        if constexpr(F::scaled) {
+          const int pair = c % ti.npair, kb = c / ti.npair;
+          const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
+          const float* sr = pair ? ti.sr[1] : ti.sr[0];
+          sc = sl[(ti.m0 >> 7) * ti.kt + kb] * sr[((ti.n0 + h * F::HALF) >> 7) * ti.kt + kb];
+        }
 #pragma unroll
         for(int j = 0; j < F::HALF / 32; ++j) {
           uint32_t r[32];
           umma::tmem_ld_32x32b_x32(base + 32 * j, r);
           umma::tmem_ld_wait();
 #pragma unroll
-          for(int i = 0; i < 32; ++i) acc[32 * j + i] = (c == 0) ? __uint_as_float(r[i]) : acc[32 * j + i] + __uint_as_float(r[i]);
+          for(int i = 0; i < 32; ++i) {
+            const float v = F::scaled ? sc * __uint_as_float(r[i]) : __uint_as_float(r[i]);
+            acc[32 * j + i] = (c == 0) ? v : acc[32 * j + i] + v;
+          }
         }
         umma::fence_before_sync();
         __syncwarp();
@@ -503,7 +576,9 @@ gbpoly_status launch_split(gbpoly_ctx* ctx, const float* X, int64_t ld, bool k_m
 template <class F>
 gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, int64_t left_rows, Panels right,
     int64_t right_rows, int64_t Kp) {
-  const auto dt = F::elem == Elem::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const auto dt = F::elem == Elem::BF16   ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                  : F::elem == Elem::TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                          : CU_TENSOR_MAP_DATA_TYPE_UINT8;
   const auto sw = F::ROW == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
   gbpoly_status st;
   for(int t = 0; t < F::terms; ++t) {
@@ -601,6 +676,60 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   return launch_tc_kernel<F>(ctx, sched, tiles, kernel_name);
 }
 
+// FP8 form: quantize both operands (panels + block scales), one MMA product.
+gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
+  using F = FormFP8;
+  if(a.M == 0 || a.N == 0) return GBPOLY_OK;
+  if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
+    return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");
+  const bool same = same_operand(a);
+  const int64_t Kp = int64_t(align_up(size_t(std::max<int64_t>(a.K, 1)), 128));
+  const int64_t mb = (a.M + 127) / 128, nb = (a.N + 127) / 128, kb = Kp / 128;
+  const size_t a_bytes = align_up(size_t(a.M) * Kp, 1024), b_bytes = same ? 0 : align_up(size_t(a.N) * Kp, 1024);
+  const size_t sa_bytes = align_up(size_t(mb * kb) * 4, 256), sb_bytes = same ? 0 : align_up(size_t(nb * kb) * 4, 256);
+  gbpoly_status st = ensure_workspace(ctx, a_bytes + b_bytes + sa_bytes + sb_bytes);
+  if(st != GBPOLY_OK) return st;
+  char* ws = static_cast<char*>(ctx->ws.ptr);
+  uint8_t* qa = reinterpret_cast<uint8_t*>(ws);
+  uint8_t* qb = same ? qa : reinterpret_cast<uint8_t*>(ws + a_bytes);
+  float* sa = reinterpret_cast<float*>(ws + a_bytes + b_bytes);
+  float* sb = same ? sa : reinterpret_cast<float*>(ws + a_bytes + b_bytes + sa_bytes);
+  static unsigned attr_q = 0;
+  constexpr int kQSmem = 128 * 129 * 4;
+  if(ctx->device < 32 && !(attr_q & (1u << ctx->device))) {
+    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(quantize_e4m3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kQSmem));
+    attr_q |= 1u << ctx->device;
+  }
+  {
+    ProfileScope prof(ctx, "quantize_e4m3");
+    quantize_e4m3_kernel<<<dim3(unsigned(kb), unsigned(mb)), 256, kQSmem, ctx->stream>>>(
+        a.A, a.lda, a.op_a == GBPOLY_OP_N ? 1 : 0, int(a.M), int(a.K), int(Kp), qa, sa);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+    if(!same) {
+      quantize_e4m3_kernel<<<dim3(unsigned(kb), unsigned(nb)), 256, kQSmem, ctx->stream>>>(
+          a.B, a.ldb, a.op_b == GBPOLY_OP_T ? 1 : 0, int(a.N), int(a.K), int(Kp), qb, sb);
+      GBPOLY_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  GemmMaps maps;
+  int npair = 1;
+  Panels pa{reinterpret_cast<char*>(qa), a_bytes}, pb{reinterpret_cast<char*>(qb), b_bytes};
+  if((st = make_product_maps<F>(ctx, maps.p[0], pa, a.M, pb, a.N, Kp)) != GBPOLY_OK) return st;
+  SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
+  sched.sl[0] = sa;
+  sched.sr[0] = sb;
+  if(a.dual) {  // syr2k: B_i . A_j^T
+    sched.npair = 2;
+    if((st = make_product_maps<F>(ctx, sched.maps.p[1], pb, a.M, pa, a.N, Kp)) != GBPOLY_OK) return st;
+    sched.sl[1] = sb;
+    sched.sr[1] = sa;
+  } else {
+    sched.maps.p[1] = sched.maps.p[0];
+  }
+  const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  return launch_tc_kernel<F>(ctx, sched, tiles, "fp8_gemm");
+}
+
 template <class F>
 size_t bytes_of(int64_t M, int64_t N, int64_t K, bool same) {
   const Layout l = layout<F>(M, N, K, same);
@@ -616,6 +745,11 @@ size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, b
   case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same);
   case GBPOLY_PREC_TF32X3: return bytes_of<FormTF32x3>(M, N, K, same);
   case GBPOLY_PREC_BF16X6: return bytes_of<FormBF16x6>(M, N, K, same);
+  case GBPOLY_PREC_FP8: {
+    const size_t Kp = align_up(size_t(std::max<int64_t>(K, 1)), 128), kb = Kp / 128;
+    return align_up(size_t(M) * Kp, 1024) + (same ? 0 : align_up(size_t(N) * Kp, 1024)) +
+           align_up(size_t((M + 127) / 128) * kb * 4, 256) + (same ? 0 : align_up(size_t((N + 127) / 128) * kb * 4, 256));
+  }
   default: return 0;
   }
 }
@@ -626,6 +760,7 @@ int tensor_config_count(gbpoly_precision prec) {
   case GBPOLY_PREC_BF16X3:
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6: return 3;
+  case GBPOLY_PREC_FP8: return 1;
   default: return 0;
   }
 }
@@ -644,6 +779,7 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form<FormBF16x6>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form<FormBF16x6_b>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form<FormBF16x6_c>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
 }

@@ -67,6 +67,16 @@ struct InstrDesc {
                                     (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
 };
 
+// Instruction descriptor for kind::f8f6f4 with E4M3 operands (format code 0)
+// and FP32 accumulation: same field positions as kind::f16.
+template <int M, int N>
+struct InstrDescE4M3 {
+  static_assert(M == 64 || M == 128, "UMMA M");
+  static_assert(N % 16 == 0 && N >= 16 && N <= 256, "UMMA N");
+  static constexpr uint32_t value = (1u << 4) | (static_cast<uint32_t>(N >> 3) << 17) |
+                                    (static_cast<uint32_t>(M >> 4) << 24);
+};
+
 // ---------------------------------------------------------------- TMEM alloc
 // Executed by all 32 lanes of one warp.  Writes the base address to smem.
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
@@ -107,6 +117,17 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint6
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// D[tmem] (+)= A * B^T, kind::f8f6f4 (8-bit operands, K = 32 per instruction).
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+    uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
       : "memory");
 }

@@ -168,3 +168,46 @@ def test_2mm_chain_passes_reference_verify(ctx, prec):
     ctx.gemm(P, n, n, n, 1.0, dC, n, dD, n, 0.0, dE, n)
     ctx.synchronize()
     assert_verify(oracle.host_mm2(n), ctx.download(dE, (n, n)))
+
+
+def _block_scaled(rng, rows, cols, lo=1e-3, hi=1e3):
+    x = rng.uniform(-1, 1, (rows, cols))
+    for r in range(0, rows, 128):
+        for c in range(0, cols, 128):
+            x[r:r + 128, c:c + 128] *= np.exp(rng.uniform(np.log(lo), np.log(hi)))
+    return x.astype(np.float32)
+
+
+@pytest.mark.parametrize("op_b", [Op.N, Op.T])
+@pytest.mark.parametrize("mnk", [(256, 384, 512), (200, 130, 300), (128, 256, 128)])
+def test_fp8_block_scaled_vs_fp64(ctx, op_b, mnk):
+    """e4m3 with one scale per 128 x 128 block: 3 mantissa bits, so a few
+    percent normwise; block-wise magnitudes spanning 1e-3..1e3 stay resolved."""
+    M, N, K = mnk
+    rng = np.random.default_rng(M + N + K)
+    A = _block_scaled(rng, M, K)
+    B = _block_scaled(rng, N, K) if op_b == Op.T else _block_scaled(rng, K, N)
+    A[:128, :128] = 0.0  # an all-zero block (scale 1)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    dev = run_gemm(ctx, A, B, C, 1.0, 0.25, op_b=op_b, prec=Precision.FP8)
+    ref = oracle.gemm_f64(A, B, C, 1.0, 0.25, op_b=int(op_b))
+    max_rel, frob, _ = oracle.error_norms(dev, ref)
+    assert frob < 6e-2, (max_rel, frob)
+
+
+def test_fp8_syrk_and_syr2k(ctx):
+    rng = np.random.default_rng(4)
+    n, k = 256, 384
+    A = rng.standard_normal((n, k)).astype(np.float32)
+    B = rng.standard_normal((n, k)).astype(np.float32)
+    C = rng.standard_normal((n, n)).astype(np.float32)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.syrk(Precision.FP8, n, k, 1.0, dA, k, 1.0, dC, n)
+    ctx.synchronize()
+    ref = oracle.gemm_f64(A, A, C, 1.0, 1.0, op_b=1)
+    assert oracle.error_norms(ctx.download(dC, C.shape), ref)[1] < 6e-2
+    ctx.h2d(dC, C)
+    ctx.syr2k(Precision.FP8, n, k, 1.0, dA, k, dB, k, 1.0, dC, n)
+    ctx.synchronize()
+    ref2 = oracle.gemm_f64(A, B, C, 1.0, 1.0, op_b=1, A2=B, B2=A)
+    assert oracle.error_norms(ctx.download(dC, C.shape), ref2)[1] < 6e-2
