@@ -193,6 +193,29 @@ def run_gpu(args, dist: Dist) -> dict | None:
     for prec in forms:
         if prec != Precision.FP32:  # tile configuration from the autotuner, before any timing
             tuned[prec] = ctx.autotune(prec, n, n, n, reps=3)[0]
+    # error of every form on seeded uniform[-1, 1] inputs too (same shape, alpha, beta)
+    rngu = np.random.default_rng(7)
+    uA, uB, uC = (rngu.uniform(-1, 1, (n, n)).astype(np.float32) for _ in range(3))
+    duA, duB, duC0, duC = ctx.upload(uA), ctx.upload(uB), ctx.upload(uC), ctx.upload(uC)
+    del uA, uB
+    dA64, dB64, dRu = ctx.alloc(2 * nbytes), ctx.alloc(2 * nbytes), ctx.alloc(2 * nbytes)
+    ctx.convert_f32_f64(duA, dA64, n * n)
+    ctx.convert_f32_f64(duB, dB64, n * n)
+    ctx.convert_f32_f64(duC0, dRu, n * n)
+    ctx.gemm_f64(n, n, n, ALPHA, dA64, n, dB64, n, BETA, dRu, n)
+    ctx.synchronize()
+    ctx.free(dA64)
+    ctx.free(dB64)
+    uniform_err = {}
+    for prec in forms:
+        ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(duC), gbpoly._ptr(duC0), nbytes)
+        ctx.gemm(prec, n, n, n, ALPHA, duA, n, duB, n, BETA, duC, n)
+        ctx.synchronize()
+        mr, fr, _ = ctx.error_norms(duC, n, dRu, n, n, n)
+        uniform_err[prec] = {"max_rel": mr, "frob_rel": fr}
+    for b in (duA, duB, duC0, duC, dRu):
+        ctx.free(b)
+
     for prec in forms:
         fresh_c()
         one(prec)
@@ -224,6 +247,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
         tiers[prec.name.lower()] = {
             "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12 * dist.world,
             "err_vs_fp64": {"max_rel": max_rel, "frob_rel": frob, "max_elem_rel": elem},
+            "err_vs_fp64_uniform_inputs": uniform_err[prec],
             "kernel_launches_per_step": sum(c for c, _ in kernels.values()) / args.steps,
             "kernels": {k: {"launches": c, "avg_ms": t / c, "share": t / sum(x[1] for x in kernels.values())}
                         for k, (c, t) in kernels.items()},
@@ -268,6 +292,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
         ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
 
     grouped = None if args.no_grouped else run_grouped_workload(ctx, args)
+    family = None if args.no_family else run_family(ctx, args)
 
     head = tiers[headline.name.lower()]
     peaks, peak_kind = load_peaks()
@@ -299,8 +324,159 @@ def run_gpu(args, dist: Dist) -> dict | None:
         "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 * dist.world, "unit": "TFLOP/s",
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
         "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
-        "device": props, "peak_kind": peak_kind, "grouped": grouped,
+        "device": props, "peak_kind": peak_kind, "grouped": grouped, "family": family,
     }
+
+
+def run_family(ctx, args) -> dict:
+    """The rest of the GEMM family at N = args.family_size, polybench inputs:
+    2mm (C += A.B; E = C.D) and 3mm (E = A.B; F = C.D; G = E.F) with the stages
+    of the tensor-core forms captured in one CUDA graph, syrk (C = a A.A^T + b C)
+    and syr2k (C = a (A.B^T + B.A^T) + b C) with a = 32412, b = 2123, and the
+    FP64 forms of syrk/syr2k timed alongside.  Errors against an FP64 chain
+    computed on the GPU: every stage of 2mm/3mm, and the final output."""
+    import gbpoly
+    from gbpoly import Precision
+
+    n = args.family_size
+    nb = n * n * 4
+    i = np.arange(n, dtype=np.float32)[:, None]
+    j = np.arange(n, dtype=np.float32)[None, :]
+    nf = np.float32(n)
+    ij = i * j
+    mats = {"ij": ij / nf, "ij1": (ij + np.float32(1)) / nf, "ij2": (ij + np.float32(2)) / nf,
+            "i(j+1)": (i * (j + np.float32(1))) / nf, "i(j+2)": (i * (j + np.float32(2))) / nf,
+            "i(j+3)": (i * (j + np.float32(3))) / nf}
+    dev = {k: ctx.upload(v) for k, v in mats.items()}
+    del mats
+    forms = [Precision.FP32, Precision.BF16X3, Precision.BF16X6]
+    work = [ctx.alloc(nb) for _ in range(3)]
+    ref64 = [ctx.alloc(2 * nb) for _ in range(4)]
+    out = {"size": n}
+
+    def to64(src, dst):
+        ctx.convert_f32_f64(src, dst, n * n)
+
+    def dgemm(a, b, c, alpha, beta, op_b=gbpoly.Op.N):
+        ctx.gemm_f64(n, n, n, alpha, a, n, b, n, beta, c, n, op_b=op_b)
+
+    def time_steps(step, flops):
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        e0, e1 = ctx.event(), ctx.event()
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        ctx.synchronize()
+        ms = e0.elapsed_ms(e1) / args.steps
+        return {"ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+
+    def err(c32, r64):
+        mr, fr, _ = ctx.error_norms(c32, n, r64, n, n, n)
+        return {"max_rel": mr, "frob_rel": fr}
+
+    def graph_of(fn):
+        ctx.graph_begin()
+        fn()
+        return ctx.graph_end()
+
+    # ---- 2mm: C += A.B (A = ij, B = i(j+1), C = i(j+3)), E = C.D (D = i(j+2))
+    A, B, Cin, D = dev["ij"], dev["i(j+1)"], dev["i(j+3)"], dev["i(j+2)"]
+    a64, b64, c64, e64 = ref64
+    to64(A, a64); to64(B, b64); to64(Cin, c64)
+    dgemm(a64, b64, c64, 1.0, 1.0)                 # stage 1 in FP64
+    to64(D, b64)
+    dgemm(c64, b64, e64, 1.0, 0.0)                 # stage 2 in FP64
+    C, E = work[0], work[1]
+    res = {}
+    for prec in forms:
+        ctx.workspace_reserve(ctx.workspace_query(prec, n, n, n))
+
+        def stages(prec=prec):
+            ctx.gemm(prec, n, n, n, 1.0, A, n, B, n, 1.0, C, n)
+            ctx.gemm(prec, n, n, n, 1.0, C, n, D, n, 0.0, E, n)
+        ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(C), gbpoly._ptr(Cin), nb)
+        stages()
+        ctx.synchronize()
+        r = {"stage1_C": err(C, c64), "end_to_end_E": err(E, e64)}
+        g = graph_of(stages) if prec != Precision.FP32 else None
+        r.update(time_steps((lambda: ctx.graph_launch(g)) if g else stages, 4.0 * n ** 3))
+        r["mode"] = "one CUDA graph" if g else "two launches"
+        if g:
+            ctx.graph_destroy(g)
+        res[prec.name.lower()] = r
+    out["2mm"] = res
+
+    # ---- 3mm: E = A.B, F = C.D, G = E.F (A = ij, B = i(j+1), C = i(j+3), D = i(j+2))
+    Cm = dev["i(j+3)"]
+    to64(A, a64); to64(B, b64)
+    dgemm(a64, b64, c64, 1.0, 0.0)                 # E64 in c64
+    to64(Cm, a64); to64(D, b64)
+    dgemm(a64, b64, e64, 1.0, 0.0)                 # F64 in e64
+    g64 = ref64[0]
+    dgemm(c64, e64, g64, 1.0, 0.0)                 # G64 (overwrites a64, no longer needed)
+    E, F, G = work
+    res = {}
+    for prec in forms:
+        def stages(prec=prec):
+            ctx.gemm(prec, n, n, n, 1.0, A, n, B, n, 0.0, E, n)
+            ctx.gemm(prec, n, n, n, 1.0, Cm, n, D, n, 0.0, F, n)
+            ctx.gemm(prec, n, n, n, 1.0, E, n, F, n, 0.0, G, n)
+        stages()
+        ctx.synchronize()
+        r = {"stage1_E": err(E, c64), "stage2_F": err(F, e64), "end_to_end_G": err(G, g64)}
+        g = graph_of(stages) if prec != Precision.FP32 else None
+        r.update(time_steps((lambda: ctx.graph_launch(g)) if g else stages, 6.0 * n ** 3))
+        r["mode"] = "one CUDA graph" if g else "three launches"
+        if g:
+            ctx.graph_destroy(g)
+        res[prec.name.lower()] = r
+    out["3mm"] = res
+
+    # ---- syrk / syr2k, alpha = 32412, beta = 2123 (A = ij, B = ij1, C = ij2), FP64 form alongside
+    al, be = 32412.0, 2123.0
+    A, B, C0 = dev["ij"], dev["ij1"], dev["ij2"]
+    C = work[0]
+    a64, b64, r64, c64w = ref64
+    to64(A, a64); to64(B, b64)
+    for name in ("syrk", "syr2k"):
+        to64(C0, r64)
+        dgemm(a64, a64 if name == "syrk" else b64, r64, al, be, op_b=gbpoly.Op.T)
+        if name == "syr2k":
+            dgemm(b64, a64, r64, al, 1.0, op_b=gbpoly.Op.T)
+        res = {}
+        flops = (2.0 if name == "syrk" else 4.0) * n ** 3  # full square, as the reference computes
+        for prec in forms:
+            def step(prec=prec):
+                if name == "syrk":
+                    ctx.syrk(prec, n, n, al, A, n, be, C, n)
+                else:
+                    ctx.syr2k(prec, n, n, al, A, n, B, n, be, C, n)
+            ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(C), gbpoly._ptr(C0), nb)
+            step()
+            ctx.synchronize()
+            r = {"output": err(C, r64)}
+            r.update(time_steps(step, flops))
+            res[prec.name.lower()] = r
+        to64(C0, c64w)
+
+        def step64():
+            if name == "syrk":
+                ctx.syrk_f64(n, n, al, a64, n, be, c64w, n)
+            else:
+                ctx.syr2k_f64(n, n, al, a64, n, b64, n, be, c64w, n)
+        saved = (args.steps, args.warmup)
+        args.steps, args.warmup = 2, 1  # the FP64 pipe is ~1/64 of FP32: two timed launches
+        res["fp64"] = time_steps(step64, flops)
+        args.steps, args.warmup = saved
+        out[name] = res
+    for b in list(dev.values()) + work + ref64:
+        ctx.free(b)
+    for k in ("2mm", "3mm", "syrk", "syr2k"):
+        out[k]["speedup_bf16x3_vs_fp32"] = out[k]["bf16x3"]["tflops"] / out[k]["fp32"]["tflops"]
+    return out
 
 
 def run_grouped_workload(ctx, args) -> dict:
@@ -435,6 +611,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-GEMM workload")
     ap.add_argument("--grouped-count", type=int, default=512)
+    ap.add_argument("--no-family", action="store_true", help="skip the 2mm/3mm/syrk/syr2k section")
+    ap.add_argument("--family-size", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist()
@@ -482,7 +660,7 @@ def main() -> None:
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
-                    peaks=res["peak_kind"], grouped=res["grouped"])
+                    peaks=res["peak_kind"], grouped=res["grouped"], family=res["family"])
         print(json.dumps(line))
     dist.close()
 
