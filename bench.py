@@ -35,9 +35,8 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of the same kernel and workload (profiles/ holds the summaries).
-# N=4096 capture: 389.6e6 bytes per bf16x3 launch (profiles/split_gemm_bf16x3_gemm_n4096.md); the N=8192
-# figure scales it by the panel bytes each tile streams (8x the FLOPs, 4x the matrix bytes): x4.
-TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {("bf16x3_gemm", 4096): 389.6e6, ("bf16x3_gemm", 8192): 4 * 389.6e6}
+# Measured with ncu on the tuned configuration (profiles/split_gemm_bf16x3_n4096_n8192.md).
+TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {("bf16x3_gemm", 4096): 397.3e6, ("bf16x3_gemm", 8192): 2.797e9}
 
 
 # ------------------------------------------------------------------ helpers
@@ -183,15 +182,20 @@ def run_gpu(args, dist: Dist) -> dict | None:
     def fresh_c():
         ctx.lib.gbpoly_memcpy_d2d(ctx.handle, gbpoly._ptr(dC), gbpoly._ptr(dC0), nbytes)
 
-    forms = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.TF32, Precision.FP8]
-    headline = Precision.BF16X3
+    forms = [Precision[f.strip().upper()] for f in args.forms.split(",")]
+    headline = Precision.BF16X3 if Precision.BF16X3 in forms else forms[-1]
     tiers = {}
     sampler = ClockSampler(dist.local_rank)
     sampler.start()
     timed_window = (0.0, 0.0)
     tuned = {}
     for prec in forms:
-        if prec != Precision.FP32:  # tile configuration from the autotuner, before any timing
+        if prec == Precision.FP32:
+            continue
+        if args.tile_config is not None:  # forced (profiling runs: no autotuner launches)
+            tuned[prec] = min(args.tile_config, ctx.config_count(prec) - 1)
+            ctx.config_set(prec, n, n, n, tuned[prec])
+        else:  # tile configuration from the autotuner, before any timing
             tuned[prec] = ctx.autotune(prec, n, n, n, reps=3)[0]
     # error of every form on seeded uniform[-1, 1] inputs too (same shape, alpha, beta)
     rngu = np.random.default_rng(7)
@@ -267,15 +271,12 @@ def run_gpu(args, dist: Dist) -> dict | None:
         gbpoly._check(ctx.lib.gbpoly_host_alloc(ctx.handle, ct.byref(p), nbytes))
         ct.memmove(p.value, arr.ctypes.data, nbytes)
         hbuf.append(p.value)
-    pout = ct.c_void_p()
-    gbpoly._check(ctx.lib.gbpoly_host_alloc(ctx.handle, ct.byref(pout), nbytes))
-    hA, hB, hC, hOut = hbuf[0], hbuf[1], hbuf[2], pout.value
+    hA, hB, hC = hbuf[0], hbuf[1], hbuf[2]
+    hOut = hC  # C is read (beta != 0) and overwritten in place, as the reference's C buffer
 
     def e2e_step():
-        for dst, src in ((dA, hA), (dB, hB), (dC, hC)):
-            gbpoly._check(ctx.lib.gbpoly_memcpy_h2d(ctx.handle, gbpoly._ptr(dst), ct.c_void_p(src), nbytes))
-        one(headline)
-        gbpoly._check(ctx.lib.gbpoly_memcpy_d2h(ctx.handle, ct.c_void_p(hOut), gbpoly._ptr(dC), nbytes))
+        # one call with host buffers: operands over the link, C back, pipelined inside the call
+        ctx.gemm_host(headline, n, n, n, ALPHA, hA, n, hB, n, BETA, hOut, n)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -288,7 +289,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     e1.record()
     ctx.synchronize()
     e2e_ms = dist.max(e0.elapsed_ms(e1) / args.steps)
-    for p in (hA, hB, hC, hOut):
+    for p in (hA, hB, hC):
         ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
 
     grouped = None if args.no_grouped else run_grouped_workload(ctx, args)
@@ -612,6 +613,8 @@ def main() -> None:
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-GEMM workload")
     ap.add_argument("--grouped-count", type=int, default=512)
     ap.add_argument("--no-family", action="store_true", help="skip the 2mm/3mm/syrk/syr2k section")
+    ap.add_argument("--forms", default="fp32,bf16x3,tf32x3,bf16x6,tf32,fp8", help="forms to time (comma list)")
+    ap.add_argument("--tile-config", type=int, default=None, help="force this tile configuration (no autotuning)")
     ap.add_argument("--family-size", type=int, default=4096)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

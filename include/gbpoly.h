@@ -178,6 +178,19 @@ gbpoly_status gbpoly_gemm_f32(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op 
     int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
     float beta, float* C, int64_t ldc);
 
+/* The same contraction with A, B and C in HOST memory (pinned memory from
+ * gbpoly_host_alloc reaches full link speed): the operands travel to the
+ * device, C comes back, all inside the call, pipelined over row panels of
+ * C so that the copies overlap the computation.  This is the whole-job form
+ * of the reference's run: setup's upload (PrefetchedBuffer::initialize,
+ * include/memory_wrappers.h:47-51), the kernel (polybench/gemm.cpp:82-91)
+ * and verify's read-back (polybench/gemm.cpp:99).  Asynchronous on the
+ * context's stream; the host buffers must stay valid until
+ * gbpoly_synchronize(). */
+gbpoly_status gbpoly_gemm_f32_host(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op op_a, gbpoly_op op_b,
+    int64_t M, int64_t N, int64_t K, float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
+    float beta, float* C, int64_t ldc);
+
 /* C <- alpha * A * A^T + beta * C over the FULL N x N square (A is N x K).
  * Replaces polybench/syrk.cpp:74-83 (alpha=123, beta=14512). */
 gbpoly_status gbpoly_syrk_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,

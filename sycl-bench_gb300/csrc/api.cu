@@ -183,6 +183,10 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if(ctx->ws.ptr) cudaFree(ctx->ws.ptr);
+  for(void* p : {ctx->stage_a, ctx->stage_b, ctx->stage_c})
+    if(p) cudaFree(p);
+  if(ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
+  if(ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
   for(auto& r : ctx->prof) {
     cudaEventDestroy(r.start);
     cudaEventDestroy(r.end);

@@ -65,6 +65,10 @@ struct gbpoly_ctx {
   std::vector<cudaEvent_t> event_pool;            // reusable events
   // tile configuration per (form, log2-bucket of M, N, K), from the autotuner
   std::map<std::tuple<int, int, int, int>, int> tuned;
+  // host-buffer calls: copy streams and device staging of the operands
+  cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
+  void *stage_a = nullptr, *stage_b = nullptr, *stage_c = nullptr;
+  size_t stage_a_bytes = 0, stage_b_bytes = 0, stage_c_bytes = 0;
 };
 
 namespace gbpoly {
@@ -129,6 +133,17 @@ int tensor_config_count(gbpoly_precision prec);
 gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, int config, const GemmF32Args& a);
 int tuned_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
 std::tuple<int, int, int, int> shape_bucket(gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
+// Row-panel execution of a tensor-core contraction (host-buffer calls): the
+// plan fixes form and configuration for the full shape; each panel call
+// splits its rows of A (and, for the first panel, all of B) and runs them.
+struct TensorPlan {
+  gbpoly_precision prec = GBPOLY_PREC_FP32;
+  int config = 0;
+  int64_t M = 0;
+};
+gbpoly_status tensor_plan(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op op_a, gbpoly_op op_b, int64_t M, int64_t N,
+    int64_t K, TensorPlan* plan);
+gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const GemmF32Args& a, bool first, int64_t r0);
 // Workspace bytes launch_gemm_tensor needs for this shape (0 for FP32).
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same_operand);
 

@@ -308,6 +308,7 @@ struct TileInfo {
   const float* sl[2];
   const float* sr[2];
   int kt;
+  bool mirror;  // symmetric update, tile strictly below the diagonal: also write its transpose
 };
 
 // One contraction: tiles in grouped raster order, tensor maps in the
@@ -321,12 +322,26 @@ struct SingleSched {
   int64_t ldc;
   const float* sl[2] = {nullptr, nullptr};
   const float* sr[2] = {nullptr, nullptr};
-  __device__ int count() const { return ((M + BM - 1) / BM) * ((N + BN - 1) / BN); }
+  // Symmetric updates (syrk, syr2k: the product is symmetric, M == N, BM == BN):
+  // only tiles on or below the diagonal are computed; the ones below it also
+  // store their transpose.
+  bool lower = false;
+  __device__ int count() const {
+    const int tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
+    return lower ? tm * (tm + 1) / 2 : tm * tn;
+  }
   __device__ TileInfo tile(int t) const {
     int tm, tn;
-    tile_coords(t, (M + BM - 1) / BM, (N + BN - 1) / BN, tm, tn);
+    if(lower) {  // row-major walk of the lower triangle: t = tm (tm + 1) / 2 + tn
+      tm = int((sqrtf(8.f * float(t) + 1.f) - 1.f) * 0.5f);
+      while(tm * (tm + 1) / 2 > t) --tm;
+      while((tm + 1) * (tm + 2) / 2 <= t) ++tm;
+      tn = t - tm * (tm + 1) / 2;
+    } else {
+      tile_coords(t, (M + BM - 1) / BM, (N + BN - 1) / BN, tm, tn);
+    }
     return TileInfo{tm * BM, tn * BN, M, N, Kp, npair, alpha, beta, C, ldc, maps.p, {sl[0], sl[1]}, {sr[0], sr[1]},
-        Kp / 128};
+        Kp / 128, lower && tm != tn};
   }
 };
 
@@ -349,7 +364,7 @@ struct GroupedSched {
     const int4 e = tiles[t];
     const GroupProblem p = probs[e.x];
     return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x,
-        {nullptr, nullptr}, {nullptr, nullptr}, 0};
+        {nullptr, nullptr}, {nullptr, nullptr}, 0, false};
   }
 };
 
@@ -541,6 +556,26 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           for(int r = 0; r < 32; ++r)
             if(r < rows) col[int64_t(r) * ldc] = fmaf(beta, cv[r], alpha * stage[r][lane]);
         }
+        if constexpr(F::BM == F::BN) {
+          if(ti.mirror) {
+          // transpose: C[n0 + 32j + r][row0 + lane] from the product element (row0 + lane, n0 + 32j + r)
+          const int mrow0 = nbase + 32 * j, mcol = row0 + lane;
+          if(mcol < M) {
+            const int rows = min(32, N - mrow0);
+            float* col = ti.C + int64_t(mrow0) * ldc + mcol;
+#pragma unroll
+            for(int half = 0; half < 32; half += 16) {  // 16 loads in flight at a time
+              float cv[16];
+#pragma unroll
+              for(int r = 0; r < 16; ++r)
+                cv[r] = (beta != 0.f && half + r < rows) ? col[int64_t(half + r) * ldc] : 0.f;
+#pragma unroll
+              for(int r = 0; r < 16; ++r)
+                if(half + r < rows) col[int64_t(half + r) * ldc] = fmaf(beta, cv[r], alpha * stage[lane][half + r]);
+            }
+          }
+          }
+        }
         __syncwarp();
       }
     }
@@ -672,7 +707,12 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   }
 
   SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
-  const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  if(F::BM == F::BN && (same || a.dual) && a.M == a.N) {  // symmetric product: lower triangle of tiles
+    const int64_t t = (a.M + F::BM - 1) / F::BM;
+    sched.lower = true;
+    tiles = t * (t + 1) / 2;
+  }
   return launch_tc_kernel<F>(ctx, sched, tiles, kernel_name);
 }
 
@@ -784,8 +824,79 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   }
 }
 
+// -------------------------------------------------- panel-wise contraction
+// One row panel [r0, r0 + a.M) of a contraction whose full A has Mfull rows:
+// the workspace holds the term panels of all of A (rows r0.. of this call)
+// followed by those of B, which the first panel splits once.
+template <class F>
+gbpoly_status run_form_panel(gbpoly_ctx* ctx, const GemmF32Args& a, int64_t Mfull, bool first, int64_t r0,
+    const char* name) {
+  const Layout lay = layout<F>(Mfull, a.N, a.K, false);
+  gbpoly_status st = ensure_workspace(ctx, lay.a_bytes + lay.b_bytes);
+  if(st != GBPOLY_OK) return st;
+  char* ws = static_cast<char*>(ctx->ws.ptr);
+  Panels pa{ws + size_t(r0) * lay.Kp * F::esz, lay.a_stride};
+  Panels pb{ws + lay.a_bytes, lay.b_stride};
+  if(first && (st = launch_split<F>(ctx, a.B, a.ldb, a.op_b == GBPOLY_OP_T, a.N, a.K, lay.Kp, pb)) != GBPOLY_OK)
+    return st;
+  if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, lay.Kp, pa)) != GBPOLY_OK) return st;
+  GemmMaps maps;
+  if((st = make_product_maps<F>(ctx, maps.p[0], pa, a.M, pb, a.N, lay.Kp)) != GBPOLY_OK) return st;
+  maps.p[1] = maps.p[0];
+  SingleSched<F::BM, F::BN> sched{maps, 1, int(a.M), int(a.N), int(lay.Kp), a.alpha, a.beta, a.C, a.ldc};
+  const int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  return launch_tc_kernel<F>(ctx, sched, tiles, name);
+}
+
+// Square-tile (BM == BN == 128) configuration of each form: symmetric
+// updates need it to compute only the lower triangle of tiles.
+namespace {
+bool config_is_square(gbpoly_precision prec, int config) {
+  switch(prec) {
+  case GBPOLY_PREC_TF32:
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_TF32X3: return config == 2;
+  case GBPOLY_PREC_BF16X6: return config == 0 || config == 1;
+  case GBPOLY_PREC_FP8: return true;
+  default: return false;
+  }
+}
+int square_config(gbpoly_precision prec) { return prec == GBPOLY_PREC_BF16X6 ? 1 : (prec == GBPOLY_PREC_FP8 ? 0 : 2); }
+}  // namespace
+
+gbpoly_status tensor_plan(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op, gbpoly_op, int64_t M, int64_t N,
+    int64_t K, TensorPlan* plan) {
+  if(tensor_config_count(prec) == 0) return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available");
+  plan->prec = prec;
+  plan->config = tuned_config(ctx, prec, M, N, K);
+  plan->M = M;
+  return GBPOLY_OK;
+}
+
+gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const GemmF32Args& a, bool first, int64_t r0) {
+  switch(plan.prec * 8 + plan.config) {
+  case GBPOLY_PREC_TF32 * 8 + 0: return run_form_panel<FormTF32>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 1: return run_form_panel<FormTF32_b>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 2: return run_form_panel<FormTF32_c>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form_panel<FormBF16x3>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form_panel<FormBF16x3_b>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form_panel<FormBF16x3_c>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form_panel<FormTF32x3>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form_panel<FormTF32x3_b>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form_panel<FormTF32x3_c>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form_panel<FormBF16x6>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form_panel<FormBF16x6_b>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form_panel<FormBF16x6_c>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);  // quantises both operands per panel
+  default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
+  }
+}
+
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
-  return launch_gemm_tensor_config(ctx, prec, tuned_config(ctx, prec, a.M, a.N, a.K), a);
+  int config = tuned_config(ctx, prec, a.M, a.N, a.K);
+  const bool symmetric = (same_operand(a) || a.dual) && a.M == a.N;
+  if(symmetric && !config_is_square(prec, config)) config = square_config(prec);
+  return launch_gemm_tensor_config(ctx, prec, config, a);
 }
 
 // ----------------------------------------------------------- grouped calls

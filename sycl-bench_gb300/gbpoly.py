@@ -102,6 +102,8 @@ SIGNATURES: dict[str, tuple] = {
                                        ct.POINTER(ct.c_int)]),
     "gbpoly_gemm_f32": (ct.c_int, [_vp, ct.c_int, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
                                    _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
+    "gbpoly_gemm_f32_host": (ct.c_int, [_vp, ct.c_int, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
+                                        _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_syrk_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, ct.c_float, _vp,
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
@@ -376,6 +378,11 @@ class Context:
     def gemm(self, prec, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, op_a=Op.N, op_b=Op.N) -> None:
         _check(self.lib.gbpoly_gemm_f32(self.handle, int(prec), int(op_a), int(op_b), M, N, K, alpha, _ptr(A), lda,
                                         _ptr(B), ldb, beta, _ptr(C), ldc))
+
+    def gemm_host(self, prec, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, op_a=Op.N, op_b=Op.N) -> None:
+        """A, B, C are host pointers (numpy arrays or ints)."""
+        _check(self.lib.gbpoly_gemm_f32_host(self.handle, int(prec), int(op_a), int(op_b), M, N, K, alpha, _ptr(A), lda,
+                                             _ptr(B), ldb, beta, _ptr(C), ldc))
 
     def syrk(self, prec, N, K, alpha, A, lda, beta, C, ldc) -> None:
         _check(self.lib.gbpoly_syrk_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, beta, _ptr(C), ldc))
