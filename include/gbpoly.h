@@ -202,6 +202,43 @@ gbpoly_status gbpoly_syrk_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N,
 gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
     const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
 
+/* --------------------------------------------------- column statistics -- */
+/* The passes of polybench/covariance.cpp and polybench/correlation.cpp that
+ * prepare their data matrix (a rows x cols block X, leading dimension ldx)
+ * for the X^T * X contraction, which is gbpoly_gemm_f32 with op_a = T,
+ * op_b = N and A == B (recognised as symmetric: lower triangle of tiles,
+ * mirrored).  FP32 throughout; sums use a fixed two-level order, so results
+ * are deterministic but not the reference's sequential row order.
+ * Asynchronous on the context's stream; the reductions use a per-context
+ * scratch that grows on the first call of a shape (not during capture). */
+
+/* mean[j] = (sum_i X[i][j]) / divisor, j < cols.
+ * Replaces CovarianceMean (polybench/covariance.cpp:84-96, divisor float_n)
+ * and CorrelationMean (polybench/correlation.cpp:111-124). */
+gbpoly_status gbpoly_column_mean_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    float divisor, float* mean);
+
+/* s = sqrt((sum_i (X[i][j] - mean[j])^2) / divisor); stddev[j] = s <= eps ? 1 : s.
+ * Replaces CorrelationStd (polybench/correlation.cpp:126-142), which divides
+ * by the double constant FLOAT_N: passing its float rounding moves the
+ * quotient by at most one unit in the last place. */
+gbpoly_status gbpoly_column_stddev_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    const float* mean, float divisor, float eps, float* stddev);
+
+/* Y[i][j] = X[i][j] - mean[j]                                  (stddev == NULL)
+ * Y[i][j] = ((X[i][j] - mean[j]) / scale_div) / stddev[j]     (otherwise)
+ * Y may be X itself (same leading dimension) or another buffer, e.g. a
+ * packed copy with a 16-byte-aligned leading dimension for the contraction.
+ * Replaces CovarianceReduce (polybench/covariance.cpp:98-106) and
+ * CorrelationReduce (polybench/correlation.cpp:144-156; scale_div is the
+ * float rounding of its sqrt(FLOAT_N)). */
+gbpoly_status gbpoly_center_columns_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    const float* mean, const float* stddev, float scale_div, float* Y, int64_t ldy);
+
+/* C[j][j] = value, j < n.  Replaces the diagonal stores of CorrelationCorr
+ * and Correlation5 (polybench/correlation.cpp:167-186). */
+gbpoly_status gbpoly_set_diagonal_f32(gbpoly_ctx* ctx, int64_t n, float value, float* C, int64_t ldc);
+
 
 /* -------------------------------------------------------------- grouped -- */
 

@@ -14,8 +14,8 @@ if [ ! -f "$REF/polybench/gemm.cpp" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
-build() {  # name macro
-  src="$REF/polybench/$1.cpp"
+build() {  # name macro [directory]
+  src="$REF/${3:-polybench}/$1.cpp"
   bin="$OUT/ref_$1"
   if [ -f "$bin" ] && [ "$bin" -nt "$src" ] && [ "$bin" -nt "$HERE/ref_driver.cpp" ] && [ "$bin" -nt "$HERE/sycl_shim/sycl/sycl.hpp" ]; then
     return 0
@@ -29,5 +29,8 @@ build 2mm REF_2MM &
 build 3mm REF_3MM &
 build syrk REF_SYRK &
 build syr2k REF_SYR2K &
+build covariance REF_COVARIANCE &
+build correlation REF_CORRELATION &
+build matmulchain REF_MATMULCHAIN runtime &
 wait
-for b in gemm 2mm 3mm syrk syr2k; do test -x "$OUT/ref_$b" || { echo "failed to build ref_$b" >&2; exit 1; }; done
+for b in gemm 2mm 3mm syrk syr2k covariance correlation matmulchain; do test -x "$OUT/ref_$b" || { echo "failed to build ref_$b" >&2; exit 1; }; done

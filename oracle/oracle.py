@@ -41,6 +41,11 @@ _SIGS = {
     "orc_error_norms": (None, [_f32p, _f64p, _L, ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
                                ct.POINTER(ct.c_double)]),
     "orc_num_threads": (ct.c_int, []),
+    "orc_covariance_init": (None, [_f32p, _L]),
+    "orc_covariance_host": (None, [_f32p, _f32p, _f32p, _L]),
+    "orc_correlation_init": (None, [_f32p, _L]),
+    "orc_correlation_host": (None, [_f32p, _f32p, _f32p, _f32p, _L]),
+    "orc_matmulchain_product": (None, [_f32p, _f32p, _f32p, _L]),
 }
 
 _lib = None
@@ -164,6 +169,44 @@ def host_syr2k(n):
 
 
 # ---- FP64 references
+def init_covariance(n):
+    """The (n+1) x (n+1) data array covariance.cpp's setup() fills."""
+    data = f32((n + 1, n + 1))
+    lib().orc_covariance_init(data, n)
+    return data
+
+
+def host_covariance(n, data=None):
+    """covariance.cpp's host loop on its own init (or on `data`): the (n+1) x (n+1) symmat."""
+    data = init_covariance(n) if data is None else np.array(data, np.float32, copy=True)
+    symmat, mean = f32((n + 1, n + 1)), f32(n + 1)
+    lib().orc_covariance_host(data, symmat, mean, n)
+    return symmat
+
+
+def init_correlation(n):
+    """The (n+1) x (n+1) data array correlation.cpp's setup() fills (row stride n)."""
+    data = f32((n + 1, n + 1))
+    lib().orc_correlation_init(data, n)
+    return data
+
+
+def host_correlation(n, data=None):
+    """correlation.cpp's host loop on its own init (or on `data`): the (n+1) x (n+1) symmat."""
+    data = init_correlation(n) if data is None else np.array(data, np.float32, copy=True)
+    mean, stddev, symmat = f32(n + 1), f32(n + 1), f32((n + 1, n + 1))
+    lib().orc_correlation_host(data, mean, stddev, symmat, n)
+    return symmat
+
+
+def matmulchain_product(a, b):
+    """matmulchain.cpp's multiply kernel (int accumulator) on n x n float matrices."""
+    n = a.shape[0]
+    c = f32((n, n))
+    lib().orc_matmulchain_product(np.ascontiguousarray(a, np.float32), np.ascontiguousarray(b, np.float32), c, n)
+    return c
+
+
 def gemm_f64(A, B, C0=None, alpha=1.0, beta=0.0, op_a=0, op_b=0, A2=None, B2=None):
     """alpha * op(A) op(B) [+ op(A2) op(B2)] + beta * C0 in float64 (FP32 inputs)."""
     A = np.ascontiguousarray(A, np.float32)

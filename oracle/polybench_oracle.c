@@ -15,6 +15,12 @@
  *   - device kernel bodies   gemm.cpp:82-91, syrk.cpp:74-83, syr2k.cpp:78-87
  *     (run on host cores: the reference's --device=cpu path)
  *   - comparator             polybench/common/polybenchUtilFuncts.h:27-42
+ *   - covariance, correlation polybench/covariance.cpp:20-60,
+ *                            polybench/correlation.cpp:23-87 (init and the
+ *                            host loop; their run() kernels perform the same
+ *                            per-element operations in the same order)
+ *   - matmulchain product    runtime/matmulchain.cpp:11-30, with its int
+ *                            accumulator
  *
  * Parallelism: OpenMP over output rows.  Each output element keeps the
  * reference's sequential k order, so results do not depend on the thread
@@ -237,6 +243,107 @@ void orc_syr2k_body(const float* A, const float* B, float* C, idx_t n, idx_t row
       float c = C[i * n + j] * beta;
       for(idx_t k = 0; k < n; k++) c += alpha * A[i * n + k] * B[j * n + k] + alpha * B[i * n + k] * A[j * n + k];
       C[i * n + j] = c;
+    }
+}
+
+/* ---------------------------------------------- covariance / correlation -- */
+/* The data and symmat arrays are (n + 1) x (n + 1), used from index 1. */
+
+static const float kCovFloatN = 3214212.01f;  /* covariance.cpp:18, a float constant */
+
+/* covariance.cpp:20-29: rows and columns 0..n-1 written, the rest left as
+ * the caller's zeros. */
+void orc_covariance_init(float* data, idx_t n) {
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) data[i * (n + 1) + j] = ((float)i * (float)j) / (float)n;
+}
+
+/* covariance.cpp:31-60: column means over rows 1..n divided by float_n,
+ * centring, then symmat[j1][j2] (j2 >= j1) as a sequential sum over rows,
+ * mirrored.  `data` is centred in place. */
+void orc_covariance_host(float* data, float* symmat, float* mean, idx_t n) {
+  const idx_t ld = n + 1;
+  for(idx_t j = 1; j <= n; j++) {
+    mean[j] = 0.0f;
+    for(idx_t i = 1; i <= n; i++) mean[j] += data[i * ld + j];
+    mean[j] /= kCovFloatN;
+  }
+  for(idx_t i = 1; i <= n; i++)
+    for(idx_t j = 1; j <= n; j++) data[i * ld + j] -= mean[j];
+#pragma omp parallel for schedule(dynamic, 4)
+  for(idx_t j1 = 1; j1 <= n; j1++)
+    for(idx_t j2 = j1; j2 <= n; j2++) {
+      float acc = 0.0f;
+      for(idx_t i = 1; i <= n; i++) acc += data[i * ld + j1] * data[i * ld + j2];
+      symmat[j1 * ld + j2] = acc;
+      symmat[j2 * ld + j1] = acc;
+    }
+}
+
+static const double kCorrFloatN = 3214212.01; /* correlation.cpp:12, a double constant */
+static const double kCorrEps = 0.005;         /* correlation.cpp:13 */
+
+/* correlation.cpp:23-33: written with a row stride of n (not n + 1) over
+ * i, j in 0..n, so each row's last value lands on the next row's first
+ * slot, which the next row then overwrites. */
+void orc_correlation_init(float* data, idx_t n) {
+  for(idx_t i = 0; i <= n; i++)
+    for(idx_t j = 0; j <= n; j++) data[i * n + j] = ((float)i * (float)j) / (float)(n + 1);
+}
+
+/* correlation.cpp:35-87.  Float and double steps as in the reference:
+ * the mean divides by (float)FLOAT_N; the variance by the double FLOAT_N,
+ * rounded back to float; sqrt of the float value; eps compared in double;
+ * the standardisation divides by the double sqrt(FLOAT_N), then by the
+ * float standard deviation.  Unit diagonal. */
+void orc_correlation_host(float* data, float* mean, float* stddev, float* symmat, idx_t n) {
+  const idx_t ld = n + 1;
+  for(idx_t j = 1; j <= n; j++) {
+    mean[j] = 0.0f;
+    for(idx_t i = 1; i <= n; i++) mean[j] += data[i * ld + j];
+    mean[j] /= (float)kCorrFloatN;
+  }
+  for(idx_t j = 1; j <= n; j++) {
+    stddev[j] = 0.0f;
+    for(idx_t i = 1; i <= n; i++) {
+      const float c = data[i * ld + j] - mean[j];
+      stddev[j] += c * c;
+    }
+    stddev[j] = (float)((double)stddev[j] / kCorrFloatN);
+    stddev[j] = (float)sqrt((double)stddev[j]);
+    stddev[j] = (double)stddev[j] <= kCorrEps ? 1.0f : stddev[j];
+  }
+  const double root_n = sqrt(kCorrFloatN);
+  for(idx_t i = 1; i <= n; i++)
+    for(idx_t j = 1; j <= n; j++) {
+      float v = data[i * ld + j] - mean[j];
+      v = (float)((double)v / root_n);
+      data[i * ld + j] = v / stddev[j];
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+  for(idx_t j1 = 1; j1 <= n - 1; j1++) {
+    symmat[j1 * ld + j1] = 1.0f;
+    for(idx_t j2 = j1 + 1; j2 <= n; j2++) {
+      float acc = 0.0f;
+      for(idx_t i = 1; i <= n; i++) acc += data[i * ld + j1] * data[i * ld + j2];
+      symmat[j1 * ld + j2] = acc;
+      symmat[j2 * ld + j1] = acc;
+    }
+  }
+  if(n >= 1) symmat[n * ld + n] = 1.0f;
+}
+
+/* ------------------------------------------------------------ matmulchain -- */
+/* runtime/matmulchain.cpp:11-30: c[i][j] = sum_k a[i][k] * b[k][j] with an
+ * int running sum: each step adds the float product to the int sum in
+ * float and truncates the result toward zero. */
+void orc_matmulchain_product(const float* a, const float* b, float* c, idx_t n) {
+#pragma omp parallel for schedule(static)
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      int sum = 0;
+      for(idx_t k = 0; k < n; k++) sum = (int)((float)sum + a[i * n + k] * b[k * n + j]);
+      c[i * n + j] = (float)sum;
     }
 }
 

@@ -5,9 +5,12 @@
 // compiled against the host-only SYCL stand-in in oracle/sycl_shim.  For a
 // size n the driver writes, as raw float32 row-major files:
 //   <out>_host.f32    the reference's host verification loop result
-//                     (gemm(), mm2_cpu(), mm3_cpu(), syrk(), syr2k())
+//                     (gemm(), mm2_cpu(), mm3_cpu(), syrk(), syr2k(),
+//                     covariance(), correlation(); matmulchain: the identity
+//                     its verify() expects)
 //   <out>_device.f32  the output buffer after the reference's run() kernels
 //                     executed on the host (its --device=cpu semantics)
+// Covariance and correlation write their (n + 1) x (n + 1) symmat arrays.
 // and prints "verify=PASS|FAIL" from the reference's own verify().
 // With --main it instead runs the reference's main() with the remaining
 // arguments (its CLI, result consumers and timing harness).
@@ -24,9 +27,23 @@
 
 #include <sycl/sycl.hpp>
 
+#if defined(REF_MATMULCHAIN)
+// runtime/matmulchain.cpp's main() ends without a return statement, which
+// only main may do; renamed, it would run off the end of an int function.
+// Its body is compiled as a void lambda instead.
+#define main(...) reference_main_unused = 0; static auto reference_main_body = [](__VA_ARGS__) -> void
+#include REF_SOURCE
+;
+#undef main
+static int reference_main(int argc, char** argv) {
+  reference_main_body(argc, argv);
+  return 0;
+}
+#else
 #define main reference_main
 #include REF_SOURCE
 #undef main
+#endif
 
 namespace {
 
@@ -52,6 +69,18 @@ const float* device_output(size_t first_buffer, size_t index) {
   return static_cast<const float*>(log.at(first_buffer + index)->data);
 }
 
+// run(events) where the benchmark records per-command events, run() otherwise
+// (include/benchmark_traits.h:9-18).
+template <class B>
+auto run_commands(B& b) -> decltype(b.run(std::declval<std::vector<sycl::event>&>()), void()) {
+  std::vector<sycl::event> events;
+  b.run(events);
+}
+template <class B>
+auto run_commands(B& b) -> decltype(b.run(), void()) {
+  b.run();
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -65,7 +94,7 @@ int main(int argc, char** argv) {
   }
   const size_t n = std::strtoull(argv[1], nullptr, 10);
   const std::string out = argv[2];
-  const size_t nn = n * n;
+  size_t nn = n * n;
 
   // 1) host verification loop, on freshly initialised inputs
   std::vector<float> host_out(nn);
@@ -114,8 +143,32 @@ int main(int argc, char** argv) {
   }
   using Bench = Polybench_Syr2k;
   const size_t out_index = 2;
+#elif defined(REF_COVARIANCE)
+  nn = (n + 1) * (n + 1);
+  {
+    std::vector<float> data(nn), symmat(nn), mean(n + 1);
+    init_arrays(data.data(), n);
+    covariance(data.data(), symmat.data(), mean.data(), n);
+    host_out = symmat;
+  }
+  using Bench = Polybench_Covariance;
+  const size_t out_index = 1;
+#elif defined(REF_CORRELATION)
+  nn = (n + 1) * (n + 1);
+  {
+    std::vector<float> data(nn), mean(n + 1), stddev(n + 1), symmat(nn);
+    init_arrays(data.data(), n);
+    correlation(data.data(), mean.data(), stddev.data(), symmat.data(), n);
+    host_out = symmat;
+  }
+  using Bench = Polybench_Correlation;
+  const size_t out_index = 3;
+#elif defined(REF_MATMULCHAIN)
+  for(size_t i = 0; i < n; ++i) host_out[i * n + i] = 1.f;
+  using Bench = MatmulChain<float>;
+  const size_t out_index = 4;
 #else
-#error "define one of REF_GEMM REF_2MM REF_3MM REF_SYRK REF_SYR2K"
+#error "define one of REF_GEMM REF_2MM REF_3MM REF_SYRK REF_SYR2K REF_COVARIANCE REF_CORRELATION REF_MATMULCHAIN"
 #endif
   write_f32(out + "_host.f32", host_out.data(), nn);
 
@@ -124,9 +177,8 @@ int main(int argc, char** argv) {
   Bench b(args);
   const size_t first = sycl::detail::buffer_log().size();
   b.setup();
-  std::vector<sycl::event> events;
   const auto t0 = std::chrono::steady_clock::now();
-  b.run(events);
+  run_commands(b);
   args.device_queue.wait_and_throw();
   const auto t1 = std::chrono::steady_clock::now();
   write_f32(out + "_device.f32", device_output(first, out_index), nn);

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <cstddef>
 #include <cstdlib>
 #include <exception>
@@ -63,6 +64,11 @@ class id : public range<D> {
 public:
   using range<D>::range;
   id() : range<D>() {}
+  friend id operator+(const id& a, const id& b) {
+    id r;
+    for(int d = 0; d < D; ++d) r[d] = a[d] + b[d];
+    return r;
+  }
 };
 
 template <int D>
@@ -71,6 +77,7 @@ public:
   std::size_t operator[](int i) const { return idx_[i]; }
   std::size_t get_id(int i) const { return idx_[i]; }
   range<D> get_range() const { return r_; }
+  operator id<D>() const { return idx_; }
   std::size_t get_linear_id() const {
     std::size_t l = 0;
     for(int i = 0; i < D; ++i) l = l * r_[i] + idx_[i];
@@ -253,6 +260,11 @@ public:
     return event{};
   }
 };
+
+// Built-in math used by the kernels (covariance/correlation): the host's
+// correctly rounded square roots.
+inline float sqrt(float x) { return std::sqrt(x); }
+inline double sqrt(double x) { return std::sqrt(x); }
 
 namespace usm {
 enum class alloc { host, device, shared, unknown };

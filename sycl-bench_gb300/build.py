@@ -5,7 +5,11 @@
 
 Outputs (git-ignored):
     sycl-bench_gb300/lib/libgbpoly.so
-    sycl-bench_gb300/bin/polybench_{gemm,2mm,3mm,syrk,syr2k}
+    sycl-bench_gb300/bin/{gemm,2mm,3mm,syrk,syr2k,covariance,correlation,matmulchain}
+
+Each executable is named after its source file, as the reference's build
+names its targets (CMakeLists.txt:149-151), so the reference's suite runner
+finds them under bin/benchmarks/<name>.
 
 Translation units compile in parallel; a unit is rebuilt only when it or a
 header it may include is newer than its object.  Host code is portable C++17
@@ -26,6 +30,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 HARNESS = PKG / "harness"
 POLY = PKG / "polybench"
+RUNTIME = PKG / "runtime"
 LIB_DIR = PKG / "lib"
 BIN_DIR = PKG / "bin"
 OBJ_DIR = PKG / "_build"
@@ -42,7 +47,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
              "-DSYCL_BENCH_HAS_FP64_SUPPORT=1", "-DSYCL_BENCH_ENABLE_QUEUE_PROFILING=1"]
 
-BENCHMARKS = ["gemm", "2mm", "3mm", "syrk", "syr2k"]
+# (source directory, name): the reference's polybench/<name>.cpp and runtime/<name>.cpp
+BENCHMARKS = [(POLY, "gemm"), (POLY, "2mm"), (POLY, "3mm"), (POLY, "syrk"), (POLY, "syr2k"),
+              (POLY, "covariance"), (POLY, "correlation"), (RUNTIME, "matmulchain")]
 
 
 def nvcc() -> str:
@@ -101,11 +108,11 @@ def build_executables() -> list[Path]:
     cuda_inc = cuda_home() / "include"
     headers = sorted(HARNESS.glob("*.h")) + sorted(POLY.glob("*.h")) + [INCLUDE / "gbpoly.h", lib]
     jobs, outs = [], []
-    for name in BENCHMARKS:
-        src = POLY / f"{name}.cpp"
+    for src_dir, name in BENCHMARKS:
+        src = src_dir / f"{name}.cpp"
         if not src.exists():
             continue
-        out = BIN_DIR / f"polybench_{name}"
+        out = BIN_DIR / name
         outs.append(out)
         if _newer(out, [src] + headers):
             jobs.append([shutil.which("g++") or "g++", *CXX_FLAGS, "-I", str(HARNESS), "-I", str(POLY),

@@ -29,23 +29,26 @@ gbpoly_status cuda_fail(cudaError_t e, const char* what) {
   return (e == cudaErrorMemoryAllocation) ? GBPOLY_ERR_NOMEM : GBPOLY_ERR_CUDA;
 }
 
-gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) {
-  if(ctx->ws.bytes >= bytes) return GBPOLY_OK;
+gbpoly_status ensure_scratch(gbpoly_ctx* ctx, Workspace& w, size_t bytes, const char* what) {
+  if(w.bytes >= bytes) return GBPOLY_OK;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   GBPOLY_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cs));
   if(cs != cudaStreamCaptureStatusNone)
-    return fail(GBPOLY_ERR_STATE, "workspace would grow during graph capture; call gbpoly_workspace_reserve first");
-  if(ctx->ws.ptr) {
+    return fail(GBPOLY_ERR_STATE, std::string(what) + " would grow during graph capture; make the same call once "
+                                                      "before capturing (or call gbpoly_workspace_reserve)");
+  if(w.ptr) {
     GBPOLY_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    GBPOLY_CUDA_TRY(cudaFree(ctx->ws.ptr));
-    ctx->ws.ptr = nullptr;
-    ctx->ws.bytes = 0;
+    GBPOLY_CUDA_TRY(cudaFree(w.ptr));
+    w.ptr = nullptr;
+    w.bytes = 0;
   }
   const size_t rounded = (bytes + (size_t(1) << 21) - 1) & ~((size_t(1) << 21) - 1);
-  GBPOLY_CUDA_TRY(cudaMalloc(&ctx->ws.ptr, rounded));
-  ctx->ws.bytes = rounded;
+  GBPOLY_CUDA_TRY(cudaMalloc(&w.ptr, rounded));
+  w.bytes = rounded;
   return GBPOLY_OK;
 }
+
+gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) { return ensure_scratch(ctx, ctx->ws, bytes, "workspace"); }
 
 namespace {
 cudaEvent_t pooled_event(gbpoly_ctx* ctx) {
@@ -183,6 +186,7 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if(ctx->ws.ptr) cudaFree(ctx->ws.ptr);
+  if(ctx->stats.ptr) cudaFree(ctx->stats.ptr);
   for(void* p : {ctx->stage_a, ctx->stage_b, ctx->stage_c})
     if(p) cudaFree(p);
   if(ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);

@@ -1,0 +1,218 @@
+// Column statistics and column normalisation for the covariance and
+// correlation benchmarks (polybench/covariance.cpp, polybench/correlation.cpp):
+// the passes that prepare the data matrix before its X^T.X contraction.
+//
+// The reference gives one work-item per column and walks the rows
+// sequentially through global memory (covariance.cpp:84-96,
+// correlation.cpp:111-142).  Here a column reduction is two launches:
+//   * partial pass: a CTA of 8 warps owns 32 adjacent columns and one chunk
+//     of rows; lane j of every warp reads column j (a warp reads 128
+//     contiguous bytes of a row), each thread keeps four independent loads
+//     in flight, and the 8 warps are combined in shared memory into one
+//     partial sum per (chunk, column);
+//   * final pass: one thread per column adds its chunks' partials in chunk
+//     order and applies the division (and, for standard deviations, the
+//     square root and the eps clamp).
+// The chunk count is chosen so that about four CTAs per SM stream the
+// matrix; the result does not depend on the launch beyond that fixed
+// summation tree (same inputs and shape, same bits).  All arithmetic is FP32.
+#include "gbpoly_internal.cuh"
+
+namespace gbpoly {
+namespace {
+
+constexpr int kColsPerBlock = 32;
+constexpr int kWarps = 8;
+
+// sum over rows [r0, r1) of f(X[r][j]) for this thread's column j, rows
+// warp, warp + 8, ... of the chunk; four loads in flight.
+template <bool CENTERED>
+__device__ __forceinline__ float column_chunk_sum(const float* __restrict__ col, int64_t ldx, int r0, int r1, int warp,
+    float m) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  int r = r0 + warp;
+  for(; r + 3 * kWarps < r1; r += 4 * kWarps) {
+    float v0 = col[int64_t(r) * ldx];
+    float v1 = col[int64_t(r + kWarps) * ldx];
+    float v2 = col[int64_t(r + 2 * kWarps) * ldx];
+    float v3 = col[int64_t(r + 3 * kWarps) * ldx];
+    if constexpr(CENTERED) {
+      v0 -= m, v1 -= m, v2 -= m, v3 -= m;
+      a0 = fmaf(v0, v0, a0), a1 = fmaf(v1, v1, a1), a2 = fmaf(v2, v2, a2), a3 = fmaf(v3, v3, a3);
+    } else {
+      a0 += v0, a1 += v1, a2 += v2, a3 += v3;
+    }
+  }
+  for(; r < r1; r += kWarps) {
+    float v = col[int64_t(r) * ldx];
+    if constexpr(CENTERED) {
+      v -= m;
+      a0 = fmaf(v, v, a0);
+    } else {
+      a0 += v;
+    }
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+// partial[chunk][j] = sum over the chunk's rows of X[r][j] (or (X[r][j] - mean[j])^2).
+template <bool CENTERED>
+__global__ void __launch_bounds__(kWarps * 32) column_partial_kernel(const float* __restrict__ X, int64_t ldx, int rows,
+    int cols, int rows_per_chunk, const float* __restrict__ mean, float* __restrict__ partial) {
+  __shared__ float red[kWarps][kColsPerBlock + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j = blockIdx.x * kColsPerBlock + lane;
+  const int r0 = blockIdx.y * rows_per_chunk, r1 = min(rows, r0 + rows_per_chunk);
+  float s = 0.f;
+  if(j < cols) s = column_chunk_sum<CENTERED>(X + j, ldx, r0, r1, warp, CENTERED ? mean[j] : 0.f);
+  red[warp][lane] = s;
+  __syncthreads();
+  if(warp == 0 && j < cols) {
+    float t = red[0][lane];
+#pragma unroll
+    for(int w = 1; w < kWarps; ++w) t += red[w][lane];
+    partial[int64_t(blockIdx.y) * cols + j] = t;
+  }
+}
+
+// out[j] = (sum of the chunks' partials) / divisor; for standard deviations
+// then sqrt, and 1 where the result is <= eps.
+template <bool STDDEV>
+__global__ void column_final_kernel(const float* __restrict__ partial, int chunks, int cols, float divisor, float eps,
+    float* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if(j >= cols) return;
+  float s = 0.f;
+  for(int c = 0; c < chunks; ++c) s += partial[int64_t(c) * cols + j];
+  s = s / divisor;
+  if constexpr(STDDEV) {
+    s = sqrtf(s);
+    s = s <= eps ? 1.f : s;
+  }
+  out[j] = s;
+}
+
+// Y[r][j] = X[r][j] - mean[j], or ((X[r][j] - mean[j]) / scale_div) / stddev[j].
+template <bool SCALED>
+__global__ void __launch_bounds__(256) center_columns_kernel(const float* X, int64_t ldx, int rows, int cols,
+    const float* __restrict__ mean, const float* __restrict__ stddev, float scale_div, float* Y, int64_t ldy,
+    int rows_per_block) {
+  const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+  if(j >= cols) return;
+  const float m = mean[j];
+  const float sd = SCALED ? stddev[j] : 1.f;
+  const int r0 = blockIdx.y * rows_per_block, r1 = min(rows, r0 + rows_per_block);
+  for(int r = r0 + (threadIdx.x >> 5); r < r1; r += 8) {
+    float v = X[int64_t(r) * ldx + j] - m;
+    if constexpr(SCALED) v = (v / scale_div) / sd;
+    Y[int64_t(r) * ldy + j] = v;
+  }
+}
+
+__global__ void set_diagonal_kernel(int64_t n, float value, float* C, int64_t ldc) {
+  for(int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    C[i * ldc + i] = value;
+}
+
+gbpoly_status check_block(const char* name, const void* p, int64_t rows, int64_t cols, int64_t ld) {
+  if(rows > 0 && cols > 0) {
+    if(!p) return fail(GBPOLY_ERR_INVALID, std::string(name) + ": null pointer");
+    if(ld < cols) return fail(GBPOLY_ERR_INVALID, std::string(name) + ": leading dimension smaller than columns");
+  }
+  return GBPOLY_OK;
+}
+
+gbpoly_status check_args(gbpoly_ctx* ctx, int64_t rows, int64_t cols) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
+  if(rows < 0 || cols < 0) return fail(GBPOLY_ERR_INVALID, "negative dimension");
+  if(rows >= (1ll << 31) || cols >= (1ll << 31)) return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large");
+  return GBPOLY_OK;
+}
+
+// Column reduction: partial pass into the context's stats scratch, final pass into out.
+template <bool STDDEV>
+gbpoly_status column_reduce(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx, const float* mean,
+    float divisor, float eps, float* out) {
+  if(cols == 0) return GBPOLY_OK;
+  const int col_blocks = int((cols + kColsPerBlock - 1) / kColsPerBlock);
+  // about four CTAs per SM, at least 64 rows per chunk
+  const int64_t want = std::max<int64_t>(1, (4ll * std::max(ctx->sm_count, 1) + col_blocks - 1) / col_blocks);
+  const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(want, (rows + 63) / 64));
+  const int rows_per_chunk = int((rows + chunks - 1) / chunks);
+  gbpoly_status st = ensure_scratch(ctx, ctx->stats, size_t(chunks) * size_t(cols) * sizeof(float), "column scratch");
+  if(st != GBPOLY_OK) return st;
+  float* partial = static_cast<float*>(ctx->stats.ptr);
+  {
+    ProfileScope prof(ctx, STDDEV ? "column_sumsq" : "column_sum");
+    column_partial_kernel<STDDEV><<<dim3(unsigned(col_blocks), unsigned(chunks)), kWarps * 32, 0, ctx->stream>>>(
+        X, ldx, int(rows), int(cols), std::max(rows_per_chunk, 1), mean, partial);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+  }
+  ProfileScope prof(ctx, STDDEV ? "column_stddev_final" : "column_mean_final");
+  column_final_kernel<STDDEV><<<unsigned((cols + 255) / 256), 256, 0, ctx->stream>>>(partial, int(rows > 0 ? chunks : 0),
+      int(cols), divisor, eps, out);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+}  // namespace
+}  // namespace gbpoly
+
+using namespace gbpoly;
+
+extern "C" {
+
+gbpoly_status gbpoly_column_mean_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    float divisor, float* mean) {
+  gbpoly_status st = check_args(ctx, rows, cols);
+  if(st != GBPOLY_OK) return st;
+  if((st = check_block("X", X, rows, cols, ldx)) != GBPOLY_OK) return st;
+  if(cols > 0 && !mean) return fail(GBPOLY_ERR_INVALID, "mean: null pointer");
+  return column_reduce<false>(ctx, rows, cols, X, ldx, nullptr, divisor, 0.f, mean);
+}
+
+gbpoly_status gbpoly_column_stddev_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    const float* mean, float divisor, float eps, float* stddev) {
+  gbpoly_status st = check_args(ctx, rows, cols);
+  if(st != GBPOLY_OK) return st;
+  if((st = check_block("X", X, rows, cols, ldx)) != GBPOLY_OK) return st;
+  if(cols > 0 && (!mean || !stddev)) return fail(GBPOLY_ERR_INVALID, "mean/stddev: null pointer");
+  return column_reduce<true>(ctx, rows, cols, X, ldx, mean, divisor, eps, stddev);
+}
+
+gbpoly_status gbpoly_center_columns_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* X, int64_t ldx,
+    const float* mean, const float* stddev, float scale_div, float* Y, int64_t ldy) {
+  gbpoly_status st = check_args(ctx, rows, cols);
+  if(st != GBPOLY_OK) return st;
+  if((st = check_block("X", X, rows, cols, ldx)) != GBPOLY_OK) return st;
+  if((st = check_block("Y", Y, rows, cols, ldy)) != GBPOLY_OK) return st;
+  if(cols > 0 && !mean) return fail(GBPOLY_ERR_INVALID, "mean: null pointer");
+  if(X == Y && ldx != ldy) return fail(GBPOLY_ERR_INVALID, "in-place centring needs ldy == ldx");
+  if(rows == 0 || cols == 0) return GBPOLY_OK;
+  constexpr int kRowsPerBlock = 64;
+  const dim3 grid(unsigned((cols + 31) / 32), unsigned((rows + kRowsPerBlock - 1) / kRowsPerBlock));
+  if(grid.y > 65535u) return fail(GBPOLY_ERR_UNSUPPORTED, "too many rows");
+  ProfileScope prof(ctx, stddev ? "normalize_columns" : "center_columns");
+  if(stddev)
+    center_columns_kernel<true><<<grid, 256, 0, ctx->stream>>>(X, ldx, int(rows), int(cols), mean, stddev, scale_div, Y,
+        ldy, kRowsPerBlock);
+  else
+    center_columns_kernel<false><<<grid, 256, 0, ctx->stream>>>(X, ldx, int(rows), int(cols), mean, nullptr, 1.f, Y,
+        ldy, kRowsPerBlock);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_set_diagonal_f32(gbpoly_ctx* ctx, int64_t n, float value, float* C, int64_t ldc) {
+  gbpoly_status st = check_args(ctx, n, n);
+  if(st != GBPOLY_OK) return st;
+  if((st = check_block("C", C, n, n, ldc)) != GBPOLY_OK) return st;
+  if(n == 0) return GBPOLY_OK;
+  ProfileScope prof(ctx, "set_diagonal");
+  set_diagonal_kernel<<<unsigned(std::min<int64_t>((n + 255) / 256, 4096)), 256, 0, ctx->stream>>>(n, value, C, ldc);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+}  // extern "C"

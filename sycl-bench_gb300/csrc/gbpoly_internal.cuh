@@ -59,6 +59,7 @@ struct gbpoly_ctx {
   int cc_major = 0, cc_minor = 0;
   char name[256] = {0};
   gbpoly::Workspace ws;
+  gbpoly::Workspace stats;  // per-chunk column partial sums (colstats.cu)
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
   bool profiling = false;
   std::vector<gbpoly::ProfileRecord> prof;        // launches since the last read
@@ -96,8 +97,11 @@ private:
   size_t index_ = size_t(-1);
 };
 
-// Grow the context workspace to at least `bytes` (synchronises when it grows).
+// Grow the context workspace to at least `bytes` (synchronises when it grows;
+// refused during stream capture).
 gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes);
+// Same rule for another per-context scratch buffer.
+gbpoly_status ensure_scratch(gbpoly_ctx* ctx, Workspace& w, size_t bytes, const char* what);
 
 // 2-D tensor map over a row-major matrix of `rows` x `cols` elements with
 // leading dimension `ld` (elements), box `box_rows` x `box_cols`.
@@ -123,6 +127,12 @@ struct GemmF32Args {
   const float* B2 = nullptr;
   int64_t ldb2 = 0;
 };
+// op(B) is op(A)^T on the same stored matrix (syrk's A.A^T, covariance's
+// X^T.X): the product is symmetric, and one set of split panels serves both
+// operands.
+inline bool symmetric_operand(const GemmF32Args& a) {
+  return !a.dual && a.A == a.B && a.lda == a.ldb && a.M == a.N && a.op_a != a.op_b;
+}
 gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
 // Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
 // term panels live in the context workspace.

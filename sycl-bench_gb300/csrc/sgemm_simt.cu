@@ -11,7 +11,9 @@
 //     registers and run FFMA over 128-bit shared-memory loads;
 //   * the epilogue applies C = alpha*acc + beta*C with bounds checks.
 // syr2k's two products (A_i.B_j + B_i.A_j) stream four tiles per stage into
-// the same accumulator.  Operands whose base or leading dimension is not
+// the same accumulator.  Symmetric updates (syrk, syr2k, X^T.X) compute only
+// the tiles on and below the diagonal; a tile below it also stores its
+// transpose (with its own beta * C term), so the full square is written.  Operands whose base or leading dimension is not
 // 16-byte aligned (TMA's rule) take a simple tiled kernel without TMA.
 #include "gbpoly_internal.cuh"
 #include "tiled_gemm.cuh"
@@ -108,12 +110,21 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
   tile_n = r / gsz;
 }
 
+// Row-major walk of the lower triangle of tiles: t = tm (tm + 1) / 2 + tn, tn <= tm.
+__device__ __forceinline__ void lower_coords(int t, int& tile_m, int& tile_n) {
+  int tm = int((sqrtf(8.f * float(t) + 1.f) - 1.f) * 0.5f);
+  while(tm * (tm + 1) / 2 > t) --tm;
+  while((tm + 1) * (tm + 2) / 2 <= t) ++tm;
+  tile_m = tm;
+  tile_n = t - tm * (tm + 1) / 2;
+}
+
 // A_KMAJ: op(A) rows are contiguous in k (op_a == N).  B_KMAJ: op(B) columns
 // are contiguous in k (op_b == T).  DUAL: syr2k, tiles A_i, B_j, B_i, A_j.
 template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
 __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
     const __grid_constant__ CUtensorMap tmB, int M, int N, int K, float alpha, float beta, float* __restrict__ C,
-    int64_t ldc, int* err) {
+    int64_t ldc, int lower, int* err) {
   constexpr int kTilesPerStage = DUAL ? 4 : 2;
   constexpr int kStageBytes = kTilesPerStage * kTileBytes;
   extern __shared__ __align__(1024) char smem_raw[];
@@ -126,8 +137,12 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
   const int warp = tid >> 5, lane = tid & 31;
   const int tiles_m = (M + kBM - 1) / kBM, tiles_n = (N + kBN - 1) / kBN;
   int tile_m, tile_n;
-  tile_coords(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
+  if(lower)
+    lower_coords(blockIdx.x, tile_m, tile_n);
+  else
+    tile_coords(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
   const int m0 = tile_m * kBM, n0 = tile_n * kBN;
+  const bool mirror = lower && tile_m != tile_n;
   const int ktiles = (K + kBK - 1) / kBK;
 
   if(tid == 0) {
@@ -206,6 +221,22 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
   if(!ok) return;
 
   // --------------------------------------------------------------- epilogue
+  if(mirror) {  // C[n][m] from the product element (m, n): the tile's transpose, strictly above the diagonal
+#pragma unroll
+    for(int j = 0; j < 8; ++j) {
+      const int n = n0 + owned_index<B_KMAJ || DUAL>(tn, j);
+      if(n >= N) continue;
+      float* crow = C + static_cast<int64_t>(n) * ldc;
+#pragma unroll
+      for(int i = 0; i < 8; ++i) {
+        const int m = m0 + owned_index<A_KMAJ || DUAL>(tm, i);
+        if(m < M) {
+          const float v = alpha * acc[i][j];
+          crow[m] = (beta != 0.f) ? fmaf(beta, crow[m], v) : v;
+        }
+      }
+    }
+  }
   constexpr bool kVecCols = !B_KMAJ && !DUAL;
   const bool vec_ok = kVecCols && ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
 #pragma unroll
@@ -252,7 +283,8 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
 }
 
 template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
-gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMap& ta, const CUtensorMap& tb) {
+gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMap& ta, const CUtensorMap& tb,
+    bool lower) {
   constexpr int kStageBytes = (DUAL ? 4 : 2) * kTileBytes;
   constexpr int kSmem = STAGES * kStageBytes + 1024 + 2 * STAGES * 8;
   auto kern = sgemm_tma_kernel<A_KMAJ, B_KMAJ, DUAL, STAGES>;
@@ -261,10 +293,14 @@ gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMa
     GBPOLY_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem));
     attr_set |= 1u << ctx->device;
   }
-  const int64_t tiles = ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN);
+  int64_t tiles = ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN);
+  if(lower) {
+    const int64_t t = (a.M + kBM - 1) / kBM;
+    tiles = t * (t + 1) / 2;
+  }
   ProfileScope prof(ctx, DUAL ? "sgemm_simt_dual" : "sgemm_simt");
   kern<<<static_cast<unsigned>(tiles), kThreads, kSmem, ctx->stream>>>(ta, tb, static_cast<int>(a.M),
-      static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc, ctx->err_dev);
+      static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc, lower ? 1 : 0, ctx->err_dev);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
 }
@@ -304,11 +340,13 @@ gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a) {
     st = make_tmap_2d(ctx, &tb, dt, 4, a.B, a.K, a.N, a.ldb, kBK, kBN, CU_TENSOR_MAP_SWIZZLE_NONE);
   if(st != GBPOLY_OK) return st;
 
-  if(a.dual) return launch_tma<true, true, true, 3>(ctx, a, ta, tb);
-  if(a_kmaj && b_kmaj) return launch_tma<true, true, false, 4>(ctx, a, ta, tb);
-  if(a_kmaj && !b_kmaj) return launch_tma<true, false, false, 4>(ctx, a, ta, tb);
-  if(!a_kmaj && b_kmaj) return launch_tma<false, true, false, 4>(ctx, a, ta, tb);
-  return launch_tma<false, false, false, 4>(ctx, a, ta, tb);
+  // Symmetric product (op(A) == op(B)^T as stored, or syr2k): lower triangle of tiles only.
+  const bool lower = a.M == a.N && (a.dual || symmetric_operand(a));
+  if(a.dual) return launch_tma<true, true, true, 3>(ctx, a, ta, tb, lower);
+  if(a_kmaj && b_kmaj) return launch_tma<true, true, false, 4>(ctx, a, ta, tb, lower);
+  if(a_kmaj && !b_kmaj) return launch_tma<true, false, false, 4>(ctx, a, ta, tb, lower);
+  if(!a_kmaj && b_kmaj) return launch_tma<false, true, false, 4>(ctx, a, ta, tb, lower);
+  return launch_tma<false, false, false, 4>(ctx, a, ta, tb, lower);
 }
 
 }  // namespace gbpoly

@@ -670,9 +670,7 @@ Layout layout(int64_t M, int64_t N, int64_t K, bool same) {
 }
 
 // syrk: both operands are the rows of A; split once
-bool same_operand(const GemmF32Args& a) {
-  return !a.dual && a.A == a.B && a.op_a == GBPOLY_OP_N && a.op_b == GBPOLY_OP_T && a.lda == a.ldb && a.M == a.N;
-}
+bool same_operand(const GemmF32Args& a) { return symmetric_operand(a); }
 
 template <class F>
 gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel_name) {

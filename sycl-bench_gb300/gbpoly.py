@@ -108,6 +108,10 @@ SIGNATURES: dict[str, tuple] = {
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
                                     ct.c_float, _vp, _c_i64]),
+    "gbpoly_column_mean_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, ct.c_float, _vp]),
+    "gbpoly_column_stddev_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_float, ct.c_float, _vp]),
+    "gbpoly_center_columns_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, ct.c_float, _vp, _c_i64]),
+    "gbpoly_set_diagonal_f32": (ct.c_int, [_vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_grouped_plan": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.POINTER(_vp)]),
     "gbpoly_grouped_run": (ct.c_int, [_vp, _vp]),
     "gbpoly_grouped_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int), ct.POINTER(ct.c_size_t)]),
@@ -390,6 +394,22 @@ class Context:
     def syr2k(self, prec, N, K, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
         _check(self.lib.gbpoly_syr2k_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta,
                                          _ptr(C), ldc))
+
+    # -- column statistics (covariance / correlation passes)
+    def column_mean(self, rows, cols, X, ldx, divisor, mean) -> None:
+        _check(self.lib.gbpoly_column_mean_f32(self.handle, rows, cols, _ptr(X), ldx, divisor, _ptr(mean)))
+
+    def column_stddev(self, rows, cols, X, ldx, mean, divisor, eps, stddev) -> None:
+        _check(self.lib.gbpoly_column_stddev_f32(self.handle, rows, cols, _ptr(X), ldx, _ptr(mean), divisor, eps,
+                                                 _ptr(stddev)))
+
+    def center_columns(self, rows, cols, X, ldx, mean, stddev, scale_div, Y, ldy) -> None:
+        _check(self.lib.gbpoly_center_columns_f32(self.handle, rows, cols, _ptr(X), ldx, _ptr(mean),
+                                                  _ptr(stddev) if stddev is not None else None, scale_div, _ptr(Y),
+                                                  ldy))
+
+    def set_diagonal(self, n, value, C, ldc) -> None:
+        _check(self.lib.gbpoly_set_diagonal_f32(self.handle, n, value, _ptr(C), ldc))
 
     # -- FP64
     def gemm_f64(self, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, op_a=Op.N, op_b=Op.N) -> None:

@@ -1,6 +1,6 @@
-"""The five drop-in executables on the GPU: every precision form verifies
-with the reference's own host loop, CSV columns are the reference's, and the
-CUDA-event kernel timings are filled."""
+"""The drop-in executables on the GPU: every precision form verifies with the
+reference's own host loop (matmulchain: its exact identity check), CSV
+columns are the reference's, and the CUDA-event kernel timings are filled."""
 import re
 import subprocess
 from pathlib import Path
@@ -14,10 +14,12 @@ BIN = ROOT / "sycl-bench_gb300" / "bin"
 GOLDEN = ROOT / "tests" / "golden"
 BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3mm", "syrk": "Polybench_Syrk",
            "syr2k": "Polybench_Syr2k"}
+FLOAT_ONLY = {"covariance": "Polybench_Covariance", "correlation": "Polybench_Correlation",
+              "matmulchain": "MatmulChain"}
 
 
 def run(bench, *args):
-    r = subprocess.run([str(BIN / f"polybench_{bench}"), *args], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([str(BIN / bench), *args], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     assert "rror" not in r.stderr, r.stderr
     return r.stdout
@@ -65,3 +67,43 @@ def test_graph_mode_verifies(bench):
     names = re.findall(r"Results for (\S+?)\*", out)
     assert names == [base + "_graph", base + "_bf16x3_graph", base + "_fp64_graph"]
     assert out.count("Verification: PASS") == 3, out
+
+
+@pytest.mark.parametrize("size", [257, 1024])
+@pytest.mark.parametrize("bench", list(FLOAT_ONLY))
+def test_float_only_benchmarks_verify_on_gpu(bench, size):
+    out = run(bench, f"--size={size}", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6")
+    names = re.findall(r"Results for (\S+?)\*", out)
+    base = FLOAT_ONLY[bench]
+    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6"]
+    assert out.count("Verification: PASS") == 4, out
+    if bench == "matmulchain":  # run() without events, as the reference
+        assert "kernel-time-mean: N/A" in out
+    else:
+        assert "kernel-time-mean: N/A" not in out
+
+
+def test_matmulchain_graph_grouped_and_seeded(tmp_path):
+    out = run("matmulchain", "--size=512", "--num-runs=2", "--graph", "--grouped", "--precision=fp32,bf16x3")
+    names = re.findall(r"Results for (\S+?)\*", out)
+    assert names == ["MatmulChain_grouped_graph", "MatmulChain_bf16x3_grouped_graph"]
+    assert out.count("Verification: PASS") == 2, out
+    out = run("matmulchain", "--size=384", "--num-runs=1", "--grouped", "--precision=tf32x3")
+    assert "Results for MatmulChain_tf32x3_grouped" in out and "Verification: PASS" in out
+    rep = tmp_path / "m.jsonl"
+    out = run("matmulchain", "--size=512", "--num-runs=1", "--init=uniform", "--precision=fp32,bf16x3",
+              f"--error-report={rep}")
+    import json
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert [r["precision"] for r in rows] == ["fp32", "bf16x3"]
+    assert all(r["frob_rel"] < 2e-5 for r in rows), rows
+
+
+@pytest.mark.parametrize("bench", ["covariance", "correlation"])
+def test_statistics_benchmarks_error_report_on_gpu(bench, tmp_path):
+    rep = tmp_path / "s.jsonl"
+    out = run(bench, "--size=1000", "--num-runs=1", "--precision=fp32,bf16x3,tf32x3", f"--error-report={rep}")
+    assert out.count("Verification: PASS") == 3, out
+    import json
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert len(rows) == 3 and all(r["frob_rel"] < 1e-5 for r in rows), rows

@@ -14,6 +14,9 @@ BIN = ROOT / "sycl-bench_gb300" / "bin"
 GOLDEN = ROOT / "tests" / "golden"
 BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3mm", "syrk": "Polybench_Syrk",
            "syr2k": "Polybench_Syr2k"}
+# benchmarks the reference builds for float only
+FLOAT_ONLY = {"covariance": "Polybench_Covariance", "correlation": "Polybench_Correlation",
+              "matmulchain": "MatmulChain"}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -26,7 +29,7 @@ def executables():
 
 
 def run(bench, *args, cwd=None):
-    r = subprocess.run([str(BIN / f"polybench_{bench}"), *args], capture_output=True, text=True, cwd=cwd,
+    r = subprocess.run([str(BIN / bench), *args], capture_output=True, text=True, cwd=cwd,
                        timeout=300)
     assert r.returncode == 0, r.stderr
     return r
@@ -43,6 +46,31 @@ def test_host_device_run_verifies(bench):
     assert f"Results for {BENCHES[bench]}" in out
     assert out.count("Verification: PASS") == 2, out   # FP32 and the fp64 variant
     assert f"Results for {BENCHES[bench]}_fp64" in out
+
+
+@pytest.mark.parametrize("bench", list(FLOAT_ONLY))
+def test_float_only_host_device_run_verifies(bench):
+    out = run(bench, "--size=48", "--device=cpu", "--num-runs=2").stdout
+    assert f"********** Results for {FLOAT_ONLY[bench]}**********" in out
+    assert out.count("Verification: PASS") == 1 and "_fp64" not in out, out
+
+
+def test_matmulchain_stdout_matches_reference():
+    # a benchmark without per-command events: the kernel-time lines stay N/A
+    ref = (GOLDEN / "reference_stdout_matmulchain.txt").read_text()
+    ours = run("matmulchain", "--size=16", "--num-runs=3", "--device=cpu").stdout
+    assert stdout_keys(ours) == stdout_keys(ref)
+    assert ours.splitlines()[0] == ref.splitlines()[0]
+    kt = [ln for ln in ours.splitlines() if ln.startswith("kernel-time")]
+    assert kt and all(ln.endswith("N/A") for ln in kt)
+
+
+@pytest.mark.parametrize("bench", ["covariance", "correlation"])
+def test_statistics_benchmarks_seeded_and_error_report(bench, tmp_path):
+    rep = tmp_path / "err.jsonl"
+    run(bench, "--size=40", "--device=cpu", "--num-runs=1", "--init=uniform", "--seed=3", f"--error-report={rep}")
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert len(rows) == 1 and rows[0]["init"] == "uniform" and rows[0]["frob_rel"] < 1e-5
 
 
 def test_stdout_result_names_match_reference():

@@ -14,7 +14,7 @@ import oracle
 GOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "reference_outputs.npz")
 SIZES = sorted({int(k.split("_")[1]) for k in GOLDEN.files})
 HOST = {"gemm": oracle.host_gemm, "2mm": oracle.host_mm2, "3mm": oracle.host_mm3, "syrk": oracle.host_syrk,
-        "syr2k": oracle.host_syr2k}
+        "syr2k": oracle.host_syr2k, "covariance": oracle.host_covariance, "correlation": oracle.host_correlation}
 
 
 def bits(x):
@@ -45,6 +45,45 @@ def test_kernel_bodies_match_reference_bitwise(n):
     lib.orc_gemm_body(A, B, C, n, 0, n, 1.0, 1.0)
     lib.orc_gemm_body(C, D, E, n, 0, n, 1.0, 0.0)
     np.testing.assert_array_equal(bits(E), bits(GOLDEN[f"2mm_{n}_device"]))
+
+
+@pytest.mark.parametrize("bench", ["covariance", "correlation"])
+@pytest.mark.parametrize("n", SIZES)
+def test_statistics_kernels_match_reference_bitwise(bench, n):
+    # the run() kernels (mean, [stddev,] reduce, contraction) perform the host
+    # loop's per-element operations in the same order: same bits on the
+    # (n + 1) x (n + 1) arrays, read from index 1
+    got = HOST[bench](n)
+    np.testing.assert_array_equal(bits(got[1:, 1:]), bits(GOLDEN[f"{bench}_{n}_device"][1:, 1:]))
+
+
+def test_correlation_init_keeps_row_stride_of_n():
+    n = 5
+    d = oracle.init_correlation(n).ravel()
+    # flat index i*n + j holds i*j/(n+1); row i's j = n slot is row i+1's j = 0 (zero) except after the last row
+    assert d[2 * n + 3] == np.float32(np.float32(2 * 3) / np.float32(n + 1))
+    assert d[3 * n] == 0.0 and d[n * n + n] == np.float32(np.float32(n * n) / np.float32(n + 1))
+    assert not d[(n + 1) * n + 1:].any()
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_matmulchain_matches_reference_on_identities(n):
+    eye = np.eye(n, dtype=np.float32)
+    p = oracle.matmulchain_product(eye, eye)
+    q = oracle.matmulchain_product(eye, eye)
+    r = oracle.matmulchain_product(p, q)
+    np.testing.assert_array_equal(bits(r), bits(GOLDEN[f"matmulchain_{n}_device"]))
+    np.testing.assert_array_equal(bits(r), bits(GOLDEN[f"matmulchain_{n}_host"]))
+
+
+def test_matmulchain_int_accumulator_truncates():
+    # matmulchain.cpp:21 accumulates into an int: 0 + 0.75 -> 0, (0 + 0.75) + 0.75 -> 0 ... for halves
+    # and quarters, while the true product (a float sum) is 1.5; only identity inputs hide it
+    a = np.full((2, 2), 0.75, np.float32)
+    b = np.full((2, 2), 1.0, np.float32)
+    assert (oracle.matmulchain_product(a, b) == 0.0).all()
+    c = np.full((2, 2), 1.5, np.float32)
+    assert (oracle.matmulchain_product(c, b) == 2.0).all()   # 0 + 1.5 -> 1, 1 + 1.5 -> 2
 
 
 def test_kernel_body_row_sample_is_a_prefix():
