@@ -2,7 +2,11 @@
  * gbpoly.h — C ABI of the GB300 (sm_103a) PolyBench dense-contraction library.
  *
  * This is the boundary that replaces the SYCL device queue of sycl-bench's
- * polybench/{gemm,2mm,3mm,syrk,syr2k}.cpp.  Every entry point takes plain
+ * polybench/{gemm,2mm,3mm,syrk,syr2k}.cpp (the dense contractions), and of
+ * their neighbours polybench/{covariance,correlation}.cpp (column
+ * statistics + a symmetric contraction), runtime/matmulchain.cpp (chained
+ * contractions) and polybench/{atax,bicg,mvt,gesummv}.cpp (matrix-vector
+ * products).  Every entry point takes plain
  * pointers and sizes, returns a gbpoly_status, and never throws.  Device
  * pointers are opaque to the caller and owned by the caller.  A context is
  * bound to one device and one CUDA stream; calls on one context are not
@@ -201,6 +205,41 @@ gbpoly_status gbpoly_syrk_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N,
  * Replaces polybench/syr2k.cpp:78-87 (alpha=1, beta=1). */
 gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N, int64_t K, float alpha,
     const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
+
+/* ------------------------------------------------------ matrix-vector -- */
+/* The BLAS-2 PolyBench benchmarks, HBM-bound: one pass over the matrix
+ * serves every product of a call.  FP32; sums in a fixed order (partials
+ * per 1024-column tile and per row group), deterministic but not the
+ * reference's sequential order.  Asynchronous on the context's stream; the
+ * partial sums use a per-context scratch that grows on the first call of a
+ * shape (not during capture). */
+
+/* y <- beta * y + alpha * op(A) x, A rows x cols (op N: x has cols entries,
+ * y rows; op T: x has rows entries, y cols).  With beta == 0, y is not read.
+ * Replaces Atax1 and Atax2 (polybench/atax.cpp:73-97: tmp += A x, then
+ * y += A^T tmp) with alpha = beta = 1. */
+gbpoly_status gbpoly_gemv_f32(gbpoly_ctx* ctx, gbpoly_op op, int64_t rows, int64_t cols, float alpha, const float* A,
+    int64_t lda, const float* x, float beta, float* y);
+
+/* One product y <- beta * y + alpha * op(A) x of a pair. */
+typedef struct {
+  gbpoly_op op;
+  float alpha, beta;
+  const float* x;
+  float* y;
+} gbpoly_gemv_term;
+
+/* One or two products of the same A in ONE pass over A (at most one with
+ * op T).  Replaces Bicg1 + Bicg2 (polybench/bicg.cpp:77-100: s += A^T r,
+ * q += A p) and Mvt1 + Mvt2 (polybench/mvt.cpp:75-98: x1 += A y1,
+ * x2 += A y2; the reference's second product uses A, not A^T). */
+gbpoly_status gbpoly_gemv_pair_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* A, int64_t lda,
+    const gbpoly_gemv_term* terms, int count);
+
+/* tmp <- tmp + A x;  y <- alpha * tmp + beta * (y + B x), in one pass over A
+ * and B.  Replaces Gesummv (polybench/gesummv.cpp:84-98, alpha = beta = 1). */
+gbpoly_status gbpoly_gesummv_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, float alpha, const float* A,
+    int64_t lda, const float* B, int64_t ldb, const float* x, float beta, float* tmp, float* y);
 
 /* --------------------------------------------------- column statistics -- */
 /* The passes of polybench/covariance.cpp and polybench/correlation.cpp that

@@ -32,5 +32,9 @@ build syr2k REF_SYR2K &
 build covariance REF_COVARIANCE &
 build correlation REF_CORRELATION &
 build matmulchain REF_MATMULCHAIN runtime &
+build atax REF_ATAX &
+build bicg REF_BICG &
+build mvt REF_MVT &
+build gesummv REF_GESUMMV &
 wait
-for b in gemm 2mm 3mm syrk syr2k covariance correlation matmulchain; do test -x "$OUT/ref_$b" || { echo "failed to build ref_$b" >&2; exit 1; }; done
+for b in gemm 2mm 3mm syrk syr2k covariance correlation matmulchain atax bicg mvt gesummv; do test -x "$OUT/ref_$b" || { echo "failed to build ref_$b" >&2; exit 1; }; done

@@ -46,6 +46,14 @@ _SIGS = {
     "orc_correlation_init": (None, [_f32p, _L]),
     "orc_correlation_host": (None, [_f32p, _f32p, _f32p, _f32p, _L]),
     "orc_matmulchain_product": (None, [_f32p, _f32p, _f32p, _L]),
+    "orc_atax_init": (None, [_f32p, _f32p, _L]),
+    "orc_atax_host": (None, [_f32p, _f32p, _f32p, _f32p, _L]),
+    "orc_bicg_init": (None, [_f32p, _f32p, _f32p, _L]),
+    "orc_bicg_host": (None, [_f32p, _f32p, _f32p, _f32p, _f32p, _L]),
+    "orc_mvt_init": (None, [_f32p, _f32p, _f32p, _f32p, _f32p, _L]),
+    "orc_mvt_host": (None, [_f32p, _f32p, _f32p, _f32p, _f32p, _L]),
+    "orc_gesummv_init": (None, [_f32p, _f32p, _f32p, _L]),
+    "orc_gesummv_host": (None, [_f32p, _f32p, _f32p, _f32p, _f32p, _L]),
 }
 
 _lib = None
@@ -205,6 +213,60 @@ def matmulchain_product(a, b):
     c = f32((n, n))
     lib().orc_matmulchain_product(np.ascontiguousarray(a, np.float32), np.ascontiguousarray(b, np.float32), c, n)
     return c
+
+
+# ---- matrix-vector benchmarks: init returns the setup() arrays, host the verify-loop outputs
+def init_atax(n):
+    x, A = f32(n), f32((n, n))
+    lib().orc_atax_init(x, A, n)
+    return A, x
+
+
+def host_atax(n):
+    A, x = init_atax(n)
+    y, tmp = f32(n), f32(n)
+    lib().orc_atax_host(A, x, y, tmp, n)
+    return y
+
+
+def init_bicg(n):
+    A, p, r = f32((n, n)), f32(n), f32(n)
+    lib().orc_bicg_init(A, p, r, n)
+    return A, p, r
+
+
+def host_bicg(n):
+    """s then q, concatenated."""
+    A, p, r = init_bicg(n)
+    s, q = f32(n), f32(n)
+    lib().orc_bicg_host(A, r, s, p, q, n)
+    return np.concatenate([s, q])
+
+
+def init_mvt(n):
+    a, x1, x2, y1, y2 = f32((n, n)), f32(n), f32(n), f32(n), f32(n)
+    lib().orc_mvt_init(a, x1, x2, y1, y2, n)
+    return a, x1, x2, y1, y2
+
+
+def host_mvt(n):
+    """x1 then x2, concatenated."""
+    a, x1, x2, y1, y2 = init_mvt(n)
+    lib().orc_mvt_host(a, x1, x2, y1, y2, n)
+    return np.concatenate([x1, x2])
+
+
+def init_gesummv(n):
+    A, B, x = f32((n, n)), f32((n, n)), f32(n)
+    lib().orc_gesummv_init(A, B, x, n)
+    return A, B, x
+
+
+def host_gesummv(n):
+    A, B, x = init_gesummv(n)
+    y, tmp = f32(n), f32(n)
+    lib().orc_gesummv_host(A, B, x, y, tmp, n)
+    return y
 
 
 def gemm_f64(A, B, C0=None, alpha=1.0, beta=0.0, op_a=0, op_b=0, A2=None, B2=None):

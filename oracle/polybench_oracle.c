@@ -21,6 +21,10 @@
  *                            per-element operations in the same order)
  *   - matmulchain product    runtime/matmulchain.cpp:11-30, with its int
  *                            accumulator
+ *   - atax, bicg, mvt,       polybench/atax.cpp:20-46, bicg.cpp:20-48,
+ *     gesummv                mvt.cpp:16-42, gesummv.cpp:30-56 (init and host
+ *                            loop; their run() kernels perform the same
+ *                            per-element operations in the same order)
  *
  * Parallelism: OpenMP over output rows.  Each output element keeps the
  * reference's sequential k order, so results do not depend on the thread
@@ -345,6 +349,90 @@ void orc_matmulchain_product(const float* a, const float* b, float* c, idx_t n) 
       for(idx_t k = 0; k < n; k++) sum = (int)((float)sum + a[i * n + k] * b[k * n + j]);
       c[i * n + j] = (float)sum;
     }
+}
+
+/* --------------------------------------------------------- matrix-vector -- */
+/* x[i] = i * M_PI in double, stored as float.  The reference's C++ builds see
+ * glibc's M_PI (its 3.14159 fallback applies only where M_PI is undefined). */
+static const double kPi = 3.14159265358979323846;
+
+/* atax.cpp:20-30 */
+void orc_atax_init(float* x, float* A, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    x[i] = (float)((double)i * kPi);
+    for(idx_t j = 0; j < n; j++) A[i * n + j] = ((float)i * (float)j) / (float)n;
+  }
+}
+
+/* atax.cpp:32-46: tmp[i] += A[i][j] x[j]; y[j] += A[i][j] tmp[i], row i by row i.
+ * y and tmp are accumulated onto the caller's values (zeros in the reference). */
+void orc_atax_host(const float* A, const float* x, float* y, float* tmp, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    for(idx_t j = 0; j < n; j++) tmp[i] += A[i * n + j] * x[j];
+    for(idx_t j = 0; j < n; j++) y[j] += A[i * n + j] * tmp[i];
+  }
+}
+
+/* bicg.cpp:20-35 */
+void orc_bicg_init(float* A, float* p, float* r, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    r[i] = (float)((double)i * kPi);
+    for(idx_t j = 0; j < n; j++) A[i * n + j] = ((float)i * (float)j) / (float)n;
+  }
+  for(idx_t i = 0; i < n; i++) p[i] = (float)((double)i * kPi);
+}
+
+/* bicg.cpp:37-48: s[j] += r[i] A[i][j]; q[i] += A[i][j] p[j]. */
+void orc_bicg_host(const float* A, const float* r, float* s, const float* p, float* q, idx_t n) {
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) {
+      s[j] += r[i] * A[i * n + j];
+      q[i] += A[i * n + j] * p[j];
+    }
+}
+
+/* mvt.cpp:16-28 */
+void orc_mvt_init(float* a, float* x1, float* x2, float* y1, float* y2, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    x1[i] = 0.0f;
+    x2[i] = 0.0f;
+    y1[i] = 1.0f;
+    y2[i] = 1.0f;
+    for(idx_t j = 0; j < n; j++) a[i * n + j] = (float)((double)(i + j) + 1.0) / (float)n;
+  }
+}
+
+/* mvt.cpp:30-42: x1 = x1 + A y1 and x2 = x2 + A y2 (both with A itself). */
+void orc_mvt_host(const float* a, float* x1, float* x2, const float* y1, const float* y2, idx_t n) {
+  for(idx_t i = 0; i < n; i++)
+    for(idx_t j = 0; j < n; j++) x1[i] = x1[i] + a[i * n + j] * y1[j];
+  for(idx_t k = 0; k < n; k++)
+    for(idx_t l = 0; l < n; l++) x2[k] = x2[k] + a[k * n + l] * y2[l];
+}
+
+/* gesummv.cpp:30-41 */
+void orc_gesummv_init(float* A, float* B, float* x, idx_t n) {
+  for(idx_t i = 0; i < n; i++) {
+    x[i] = 1.0f;
+    for(idx_t j = 0; j < n; j++) {
+      A[i * n + j] = 2.0f;
+      B[i * n + j] = 3.0f;
+    }
+  }
+}
+
+/* gesummv.cpp:43-56, ALPHA = BETA = 1 (float constants). */
+void orc_gesummv_host(const float* A, const float* B, const float* x, float* y, float* tmp, idx_t n) {
+  const float alpha = 1.0f, beta = 1.0f;
+  for(idx_t i = 0; i < n; i++) {
+    tmp[i] = 0.0f;
+    y[i] = 0.0f;
+    for(idx_t j = 0; j < n; j++) {
+      tmp[i] = A[i * n + j] * x[j] + tmp[i];
+      y[i] = B[i * n + j] * x[j] + y[i];
+    }
+    y[i] = alpha * tmp[i] + beta * y[i];
+  }
 }
 
 /* ---------------------------------------------------------- FP64 oracles -- */

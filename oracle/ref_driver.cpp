@@ -10,7 +10,10 @@
 //                     its verify() expects)
 //   <out>_device.f32  the output buffer after the reference's run() kernels
 //                     executed on the host (its --device=cpu semantics)
-// Covariance and correlation write their (n + 1) x (n + 1) symmat arrays.
+// Covariance and correlation write their (n + 1) x (n + 1) symmat arrays;
+// the matrix-vector benchmarks their output vectors (bicg: s then q; mvt: x1
+// then x2).  The device output is read from the buffers setup() created, by
+// creation index.
 // and prints "verify=PASS|FAIL" from the reference's own verify().
 // With --main it instead runs the reference's main() with the remaining
 // arguments (its CLI, result consumers and timing harness).
@@ -63,12 +66,6 @@ BenchmarkArgs make_args(size_t n) {
   return BenchmarkCommandLine{4, const_cast<char**>(argv)}.getBenchmarkArgs();
 }
 
-// Output buffer of the benchmark object: the k-th buffer created by setup().
-const float* device_output(size_t first_buffer, size_t index) {
-  auto& log = sycl::detail::buffer_log();
-  return static_cast<const float*>(log.at(first_buffer + index)->data);
-}
-
 // run(events) where the benchmark records per-command events, run() otherwise
 // (include/benchmark_traits.h:9-18).
 template <class B>
@@ -106,7 +103,7 @@ int main(int argc, char** argv) {
     host_out = C;
   }
   using Bench = Polybench_Gemm;
-  const size_t out_index = 2;
+  const std::vector<size_t> out_index = {2};
 #elif defined(REF_2MM)
   {
     std::vector<float> A(nn), B(nn), C(nn), D(nn), E(nn);
@@ -115,7 +112,7 @@ int main(int argc, char** argv) {
     host_out = E;
   }
   using Bench = Polybench_2mm;
-  const size_t out_index = 4;
+  const std::vector<size_t> out_index = {4};
 #elif defined(REF_3MM)
   {
     std::vector<float> A(nn), B(nn), C(nn), D(nn), E(nn), F(nn), G(nn);
@@ -124,7 +121,7 @@ int main(int argc, char** argv) {
     host_out = G;
   }
   using Bench = Polybench_3mm;
-  const size_t out_index = 6;
+  const std::vector<size_t> out_index = {6};
 #elif defined(REF_SYRK)
   {
     std::vector<float> A(nn), C(nn);
@@ -133,7 +130,7 @@ int main(int argc, char** argv) {
     host_out = C;
   }
   using Bench = Polybench_Syrk;
-  const size_t out_index = 1;
+  const std::vector<size_t> out_index = {1};
 #elif defined(REF_SYR2K)
   {
     std::vector<float> A(nn), B(nn), C(nn);
@@ -142,7 +139,7 @@ int main(int argc, char** argv) {
     host_out = C;
   }
   using Bench = Polybench_Syr2k;
-  const size_t out_index = 2;
+  const std::vector<size_t> out_index = {2};
 #elif defined(REF_COVARIANCE)
   nn = (n + 1) * (n + 1);
   {
@@ -152,7 +149,7 @@ int main(int argc, char** argv) {
     host_out = symmat;
   }
   using Bench = Polybench_Covariance;
-  const size_t out_index = 1;
+  const std::vector<size_t> out_index = {1};
 #elif defined(REF_CORRELATION)
   nn = (n + 1) * (n + 1);
   {
@@ -162,15 +159,53 @@ int main(int argc, char** argv) {
     host_out = symmat;
   }
   using Bench = Polybench_Correlation;
-  const size_t out_index = 3;
+  const std::vector<size_t> out_index = {3};
 #elif defined(REF_MATMULCHAIN)
   for(size_t i = 0; i < n; ++i) host_out[i * n + i] = 1.f;
   using Bench = MatmulChain<float>;
-  const size_t out_index = 4;
+  const std::vector<size_t> out_index = {4};
+#elif defined(REF_ATAX)
+  {
+    std::vector<float> A(nn), x(n), y(n), tmp(n);
+    init_array(x.data(), A.data(), n);
+    atax_cpu(A.data(), x.data(), y.data(), tmp.data(), n);
+    host_out = y;
+  }
+  using Bench = Polybench_Atax;
+  const std::vector<size_t> out_index = {2};
+#elif defined(REF_BICG)
+  {
+    std::vector<float> A(nn), p(n), r(n), s(n), q(n);
+    init_array(A.data(), p.data(), r.data(), n);
+    bicg_cpu(A.data(), r.data(), s.data(), p.data(), q.data(), n);
+    host_out = s;
+    host_out.insert(host_out.end(), q.begin(), q.end());
+  }
+  using Bench = Polybench_Bicg;
+  const std::vector<size_t> out_index = {2, 4};
+#elif defined(REF_MVT)
+  {
+    std::vector<float> a(nn), x1(n), x2(n), y1(n), y2(n);
+    init_arrays(a.data(), x1.data(), x2.data(), y1.data(), y2.data(), n);
+    runMvt(a.data(), x1.data(), x2.data(), y1.data(), y2.data(), n);
+    host_out = x1;
+    host_out.insert(host_out.end(), x2.begin(), x2.end());
+  }
+  using Bench = Polybench_Mvt;
+  const std::vector<size_t> out_index = {1, 2};
+#elif defined(REF_GESUMMV)
+  {
+    std::vector<float> A(nn), B(nn), x(n), y(n), tmp(n);
+    init(A.data(), B.data(), x.data(), n);
+    gesummv(A.data(), B.data(), x.data(), y.data(), tmp.data(), n);
+    host_out = y;
+  }
+  using Bench = Polybench_Gesummv;
+  const std::vector<size_t> out_index = {3};
 #else
-#error "define one of REF_GEMM REF_2MM REF_3MM REF_SYRK REF_SYR2K REF_COVARIANCE REF_CORRELATION REF_MATMULCHAIN"
+#error "define the REF_<benchmark> macro of the included source"
 #endif
-  write_f32(out + "_host.f32", host_out.data(), nn);
+  write_f32(out + "_host.f32", host_out.data(), host_out.size());
 
   // 2) the benchmark's own setup / run / verify with the kernels on the host
   BenchmarkArgs args = make_args(n);
@@ -181,7 +216,13 @@ int main(int argc, char** argv) {
   run_commands(b);
   args.device_queue.wait_and_throw();
   const auto t1 = std::chrono::steady_clock::now();
-  write_f32(out + "_device.f32", device_output(first, out_index), nn);
+  std::vector<float> dev_out;
+  for(size_t idx : out_index) {
+    const auto& st = *sycl::detail::buffer_log().at(first + idx);
+    const float* p = static_cast<const float*>(st.data);
+    dev_out.insert(dev_out.end(), p, p + st.count);
+  }
+  write_f32(out + "_device.f32", dev_out.data(), dev_out.size());
   VerificationSetting vs{true, {0, 0, 0}, {1, 1, 1}};
   const bool ok = b.verify(vs);
   std::printf("verify=%s kernel_seconds=%.6f\n", ok ? "PASS" : "FAIL",

@@ -5,7 +5,8 @@
 
 Outputs (git-ignored):
     sycl-bench_gb300/lib/libgbpoly.so
-    sycl-bench_gb300/bin/{gemm,2mm,3mm,syrk,syr2k,covariance,correlation,matmulchain}
+    sycl-bench_gb300/bin/{gemm,2mm,3mm,syrk,syr2k,covariance,correlation,matmulchain,
+                          atax,bicg,mvt,gesummv}
 
 Each executable is named after its source file, as the reference's build
 names its targets (CMakeLists.txt:149-151), so the reference's suite runner
@@ -49,7 +50,8 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wn
 
 # (source directory, name): the reference's polybench/<name>.cpp and runtime/<name>.cpp
 BENCHMARKS = [(POLY, "gemm"), (POLY, "2mm"), (POLY, "3mm"), (POLY, "syrk"), (POLY, "syr2k"),
-              (POLY, "covariance"), (POLY, "correlation"), (RUNTIME, "matmulchain")]
+              (POLY, "covariance"), (POLY, "correlation"), (RUNTIME, "matmulchain"),
+              (POLY, "atax"), (POLY, "bicg"), (POLY, "mvt"), (POLY, "gesummv")]
 
 
 def nvcc() -> str:

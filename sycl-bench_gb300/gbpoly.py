@@ -63,6 +63,12 @@ class GemmDesc(ct.Structure):
                 ("alpha", ct.c_float), ("beta", ct.c_float), ("A", ct.c_void_p), ("lda", ct.c_int64),
                 ("B", ct.c_void_p), ("ldb", ct.c_int64), ("C", ct.c_void_p), ("ldc", ct.c_int64)]
 
+class GemvTerm(ct.Structure):
+    """gbpoly_gemv_term: y = beta * y + alpha * op(A) x."""
+    _fields_ = [("op", ct.c_int), ("alpha", ct.c_float), ("beta", ct.c_float), ("x", ct.c_void_p),
+                ("y", ct.c_void_p)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/gbpoly.h
 SIGNATURES: dict[str, tuple] = {
     "gbpoly_init": (ct.c_int, [ct.c_int, ct.POINTER(_vp)]),
@@ -108,6 +114,10 @@ SIGNATURES: dict[str, tuple] = {
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
                                     ct.c_float, _vp, _c_i64]),
+    "gbpoly_gemv_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, ct.c_float, _vp]),
+    "gbpoly_gemv_pair_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_int]),
+    "gbpoly_gesummv_f32": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64, _vp, ct.c_float, _vp,
+                                      _vp]),
     "gbpoly_column_mean_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, ct.c_float, _vp]),
     "gbpoly_column_stddev_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_float, ct.c_float, _vp]),
     "gbpoly_center_columns_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, ct.c_float, _vp, _c_i64]),
@@ -394,6 +404,21 @@ class Context:
     def syr2k(self, prec, N, K, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
         _check(self.lib.gbpoly_syr2k_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta,
                                          _ptr(C), ldc))
+
+    # -- matrix-vector products (atax, bicg, mvt, gesummv)
+    def gemv(self, op, rows, cols, alpha, A, lda, x, beta, y) -> None:
+        _check(self.lib.gbpoly_gemv_f32(self.handle, int(op), rows, cols, alpha, _ptr(A), lda, _ptr(x), beta, _ptr(y)))
+
+    def gemv_pair(self, rows, cols, A, lda, terms) -> None:
+        """terms: up to two (op, alpha, beta, x, y) tuples, all over one pass of A."""
+        arr = (GemvTerm * len(terms))()
+        for t, (op, alpha, beta, x, y) in zip(arr, terms):
+            t.op, t.alpha, t.beta, t.x, t.y = int(op), alpha, beta, _ptr(x).value, _ptr(y).value
+        _check(self.lib.gbpoly_gemv_pair_f32(self.handle, rows, cols, _ptr(A), lda, ct.cast(arr, _vp), len(terms)))
+
+    def gesummv(self, rows, cols, alpha, A, lda, B, ldb, x, beta, tmp, y) -> None:
+        _check(self.lib.gbpoly_gesummv_f32(self.handle, rows, cols, alpha, _ptr(A), lda, _ptr(B), ldb, _ptr(x), beta,
+                                           _ptr(tmp), _ptr(y)))
 
     # -- column statistics (covariance / correlation passes)
     def column_mean(self, rows, cols, X, ldx, divisor, mean) -> None:

@@ -93,6 +93,14 @@ inline std::vector<gbpoly_precision> precisions(const BenchmarkArgs& args) {
   return out;
 }
 
+// The matrix-vector benchmarks run the plain FP32 form only (HBM-bound, no
+// contraction for the tensor cores): --precision may name fp32 alone.
+inline void require_fp32_only(const BenchmarkArgs& args) {
+  for(auto p : precisions(args))
+    if(p != GBPOLY_PREC_FP32)
+      throw std::invalid_argument{"--precision: this benchmark has the fp32 form only"};
+}
+
 inline Options options(const BenchmarkArgs& args, gbpoly_precision prec) {
   Options o;
   o.precision = prec;

@@ -8,7 +8,8 @@ machine), and stores:
                             <bench>_<n>_host    its host verification loop result
                                                 (matmulchain: the identity its verify expects)
                             <bench>_<n>_device  its run() kernels' output (host execution)
-                          covariance and correlation arrays are (n + 1) x (n + 1)
+                          covariance and correlation arrays are (n + 1) x (n + 1);
+                          atax, gesummv: y; bicg: s then q; mvt: x1 then x2
   reference_stdout_gemm.txt  its main() output with --output=stdio
   reference_csv_gemm.txt     its main() output with --output=<csv file> (two flushes)
   reference_stdout_matmulchain.txt  runtime/matmulchain.cpp's main() output (a
@@ -27,8 +28,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 REF_BIN = ROOT / "oracle" / "_ref"
-BENCHES = ["gemm", "2mm", "3mm", "syrk", "syr2k", "covariance", "correlation", "matmulchain"]
+BENCHES = ["gemm", "2mm", "3mm", "syrk", "syr2k", "covariance", "correlation", "matmulchain", "atax", "bicg", "mvt",
+           "gesummv"]
 PADDED = {"covariance", "correlation"}  # (n + 1) x (n + 1) arrays
+VECTORS = {"atax", "bicg", "mvt", "gesummv"}  # output vectors (bicg: s then q; mvt: x1 then x2)
 SIZES = [1, 2, 7, 16, 37, 64]
 
 
@@ -45,7 +48,8 @@ def main() -> None:
                     sys.exit(f"reference verify failed for {b} n={n}: {r.stdout}")
                 m = n + 1 if b in PADDED else n
                 for kind in ("host", "device"):
-                    arrays[f"{b}_{n}_{kind}"] = np.fromfile(f"{prefix}_{kind}.f32", np.float32).reshape(m, m)
+                    a = np.fromfile(f"{prefix}_{kind}.f32", np.float32)
+                    arrays[f"{b}_{n}_{kind}"] = a if b in VECTORS else a.reshape(m, m)
         np.savez_compressed(HERE / "reference_outputs.npz", **arrays)
 
         out = subprocess.run([str(REF_BIN / "ref_gemm"), "--main", "--size=16", "--num-runs=3"], check=True,

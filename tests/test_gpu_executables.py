@@ -16,6 +16,7 @@ BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3
            "syr2k": "Polybench_Syr2k"}
 FLOAT_ONLY = {"covariance": "Polybench_Covariance", "correlation": "Polybench_Correlation",
               "matmulchain": "MatmulChain"}
+MATVEC = {"atax": "Polybench_Atax", "bicg": "Polybench_Bicg", "mvt": "Polybench_Mvt", "gesummv": "Polybench_Gesummv"}
 
 
 def run(bench, *args):
@@ -107,3 +108,16 @@ def test_statistics_benchmarks_error_report_on_gpu(bench, tmp_path):
     import json
     rows = [json.loads(x) for x in rep.read_text().splitlines()]
     assert len(rows) == 3 and all(r["frob_rel"] < 1e-5 for r in rows), rows
+
+
+@pytest.mark.parametrize("size", [1024, 4099])
+@pytest.mark.parametrize("bench", list(MATVEC))
+def test_matrix_vector_benchmarks_verify_on_gpu(bench, size, tmp_path):
+    rep = tmp_path / "v.jsonl"
+    out = run(bench, f"--size={size}", "--num-runs=3", f"--error-report={rep}")
+    assert f"Results for {MATVEC[bench]}*" in out
+    assert out.count("Verification: PASS") == 1, out
+    assert "kernel-time-mean: N/A" not in out and "[GiB/s]" in out
+    import json
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert rows and all(r["frob_rel"] < 1e-5 for r in rows), rows

@@ -16,7 +16,8 @@ BENCHES = {"gemm": "Polybench_Gemm", "2mm": "Polybench_2mm", "3mm": "Polybench_3
            "syr2k": "Polybench_Syr2k"}
 # benchmarks the reference builds for float only
 FLOAT_ONLY = {"covariance": "Polybench_Covariance", "correlation": "Polybench_Correlation",
-              "matmulchain": "MatmulChain"}
+              "matmulchain": "MatmulChain", "atax": "Polybench_Atax", "bicg": "Polybench_Bicg", "mvt": "Polybench_Mvt",
+              "gesummv": "Polybench_Gesummv"}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -71,6 +72,16 @@ def test_statistics_benchmarks_seeded_and_error_report(bench, tmp_path):
     run(bench, "--size=40", "--device=cpu", "--num-runs=1", "--init=uniform", "--seed=3", f"--error-report={rep}")
     rows = [json.loads(x) for x in rep.read_text().splitlines()]
     assert len(rows) == 1 and rows[0]["init"] == "uniform" and rows[0]["frob_rel"] < 1e-5
+
+
+@pytest.mark.parametrize("bench", ["atax", "bicg", "mvt", "gesummv"])
+def test_matrix_vector_benchmarks_fp32_only_and_error_report(bench, tmp_path):
+    assert "fp32 form only" in run(bench, "--size=16", "--device=cpu", "--precision=bf16x3").stderr
+    rep = tmp_path / "e.jsonl"
+    out = run(bench, "--size=64", "--device=cpu", "--num-runs=1", "--init=normal", f"--error-report={rep}").stdout
+    assert "GiB/s" in out
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert len(rows) == 1 and rows[0]["frob_rel"] < 1e-5
 
 
 def test_stdout_result_names_match_reference():

@@ -14,7 +14,8 @@ import oracle
 GOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "reference_outputs.npz")
 SIZES = sorted({int(k.split("_")[1]) for k in GOLDEN.files})
 HOST = {"gemm": oracle.host_gemm, "2mm": oracle.host_mm2, "3mm": oracle.host_mm3, "syrk": oracle.host_syrk,
-        "syr2k": oracle.host_syr2k, "covariance": oracle.host_covariance, "correlation": oracle.host_correlation}
+        "syr2k": oracle.host_syr2k, "covariance": oracle.host_covariance, "correlation": oracle.host_correlation,
+        "atax": oracle.host_atax, "bicg": oracle.host_bicg, "mvt": oracle.host_mvt, "gesummv": oracle.host_gesummv}
 
 
 def bits(x):
@@ -55,6 +56,13 @@ def test_statistics_kernels_match_reference_bitwise(bench, n):
     # (n + 1) x (n + 1) arrays, read from index 1
     got = HOST[bench](n)
     np.testing.assert_array_equal(bits(got[1:, 1:]), bits(GOLDEN[f"{bench}_{n}_device"][1:, 1:]))
+
+
+@pytest.mark.parametrize("bench", ["atax", "bicg", "mvt", "gesummv"])
+@pytest.mark.parametrize("n", SIZES)
+def test_matrix_vector_kernels_match_reference_bitwise(bench, n):
+    # each run() kernel walks its row or column in the host loop's order
+    np.testing.assert_array_equal(bits(HOST[bench](n)), bits(GOLDEN[f"{bench}_{n}_device"]))
 
 
 def test_correlation_init_keeps_row_stride_of_n():
