@@ -294,6 +294,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
 
     grouped = None if args.no_grouped else run_grouped_workload(ctx, args)
     family = None if args.no_family else run_family(ctx, args)
+    neighbours = None if args.no_neighbours else run_neighbours(ctx, args)
 
     head = tiers[headline.name.lower()]
     peaks, peak_kind = load_peaks()
@@ -326,6 +327,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
         "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
         "device": props, "peak_kind": peak_kind, "grouped": grouped, "family": family,
+        "neighbours": neighbours,
     }
 
 
@@ -333,8 +335,8 @@ def run_family(ctx, args) -> dict:
     """The rest of the GEMM family at N = args.family_size, polybench inputs:
     2mm (C += A.B; E = C.D) and 3mm (E = A.B; F = C.D; G = E.F) with the stages
     of the tensor-core forms captured in one CUDA graph, syrk (C = a A.A^T + b C)
-    and syr2k (C = a (A.B^T + B.A^T) + b C) with a = 32412, b = 2123, and the
-    FP64 forms of syrk/syr2k timed alongside.  Errors against an FP64 chain
+    and syr2k (C = a (A.B^T + B.A^T) + b C) with a = 32412, b = 2123 (rates in
+    unique-output FLOPs), and the FP64 forms of syrk/syr2k timed alongside.  Errors against an FP64 chain
     computed on the GPU: every stage of 2mm/3mm, and the final output."""
     import gbpoly
     from gbpoly import Precision
@@ -448,7 +450,9 @@ def run_family(ctx, args) -> dict:
         if name == "syr2k":
             dgemm(b64, a64, r64, al, 1.0, op_b=gbpoly.Op.T)
         res = {}
-        flops = (2.0 if name == "syrk" else 4.0) * n ** 3  # full square, as the reference computes
+        # unique-output FLOPs: n (n + 1) / 2 outputs of 2n (syrk) or 4n (syr2k) FLOPs; both forms compute
+        # the lower triangle of tiles and mirror it, so the full-square count would overstate the rate
+        flops = (1.0 if name == "syrk" else 2.0) * n * n * (n + 1)
         for prec in forms:
             def step(prec=prec):
                 if name == "syrk":
@@ -477,6 +481,189 @@ def run_family(ctx, args) -> dict:
         ctx.free(b)
     for k in ("2mm", "3mm", "syrk", "syr2k"):
         out[k]["speedup_bf16x3_vs_fp32"] = out[k]["bf16x3"]["tflops"] / out[k]["fp32"]["tflops"]
+    return out
+
+
+def run_neighbours(ctx, args) -> dict:
+    """The benchmarks beside the contraction family, on their own inputs:
+      * covariance and correlation at N = args.family_size: column statistics,
+        centring into a packed copy and the symmetric X^T.X contraction (fp32,
+        bf16x3, tf32x3), unique-output FLOPs, error against an FP64 pipeline
+        (statistics in numpy FP64, contraction by DGEMM on the GPU);
+      * matmulchain at N = args.family_size: R = (A.B).(C.D) on identities
+        (exact result checked), fp32 as three launches, bf16x3 as one graph of
+        a grouped P/Q launch and the R launch;
+      * atax at N = 4096 and bicg, mvt, gesummv at N = 16384 (the suite
+        runner's sizes, bin/run-suite): matrix bytes over time against the
+        HBM peak, launches back to back."""
+    import gbpoly
+    from gbpoly import Op, Precision
+
+    n = args.family_size
+    out = {"size": n}
+    peaks, _ = load_peaks()
+    hbm = peaks.get("hbm_gbs")
+
+    def time_steps(step, steps=None, warmup=None):
+        steps, warmup = steps or args.steps, warmup or args.warmup
+        for _ in range(warmup):
+            step()
+        ctx.synchronize()
+        e0, e1 = ctx.event(), ctx.event()
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        ctx.synchronize()
+        ms = e0.elapsed_ms(e1) / steps
+        e0.destroy()
+        e1.destroy()
+        return ms
+
+    # ---- covariance / correlation: (n+1) x (n+1) arrays used from index 1
+    ld, ldp = n + 1, (n + 31) // 32 * 32
+    i = np.arange(n + 1, dtype=np.float32)
+    cov = np.zeros((ld, ld), np.float32)
+    cov[:n, :n] = (i[:n, None] * i[None, :n]) / np.float32(n)             # covariance.cpp:20-29
+    flat = np.zeros(ld * ld, np.float32)
+    for r in range(n + 1):                                               # correlation.cpp:23-33 (row stride n)
+        flat[r * n: r * n + n + 1] = (np.float32(r) * i) / np.float32(n + 1)
+    corr = flat.reshape(ld, ld)
+    del flat
+    float_n = 3214212.01
+    stats = {}
+    for name, data in (("covariance", cov), ("correlation", corr)):
+        x = data[1:, 1:].astype(np.float64)
+        x = x - x.sum(axis=0) / float(np.float32(float_n))
+        if name == "correlation":
+            sd = np.sqrt((x * x).sum(axis=0) / float_n)
+            sd[sd <= 0.005] = 1.0
+            x = x / np.sqrt(float_n) / sd
+        dX64, dR64 = ctx.upload(np.ascontiguousarray(x)), ctx.alloc(n * n * 8)
+        del x
+        ctx.gemm_f64(n, n, n, 1.0, dX64, n, dX64, n, 0.0, dR64, n, op_a=Op.T)
+        ctx.free(dX64)
+        dD, dMu, dSd = ctx.upload(data), ctx.alloc(ld * 4), ctx.alloc(ld * 4)
+        dS, dY = ctx.alloc(ld * ld * 4), ctx.alloc(n * ldp * 4)
+        ctx.lib.gbpoly_memset(ctx.handle, gbpoly._ptr(dS), 0, ld * ld * 4)
+        X, mu, sdp, S = dD.ptr + (ld + 1) * 4, dMu.ptr + 4, dSd.ptr + 4, dS.ptr + (ld + 1) * 4
+        res = {}
+        for prec in (Precision.FP32, Precision.BF16X3, Precision.TF32X3):
+            def step(prec=prec):
+                ctx.column_mean(n, n, X, ld, np.float32(float_n), mu)
+                if name == "correlation":
+                    ctx.column_stddev(n, n, X, ld, mu, np.float32(float_n), np.float32(0.005), sdp)
+                    ctx.center_columns(n, n, X, ld, mu, sdp, np.float32(np.sqrt(float_n)), dY, ldp)
+                else:
+                    ctx.center_columns(n, n, X, ld, mu, None, 1.0, dY, ldp)
+                ctx.gemm(prec, n, n, n, 1.0, dY, ldp, dY, ldp, 0.0, S, ld, op_a=Op.T, op_b=Op.N)
+                if name == "correlation":
+                    ctx.set_diagonal(n, 1.0, S, ld)
+            step()
+            ctx.synchronize()
+            got = ctx.download(dS, (ld, ld))[1:, 1:]
+            ref = ctx.download(dR64, (n, n), np.float64)
+            if name == "correlation":
+                np.fill_diagonal(ref, 1.0)
+            e = got.astype(np.float64) - ref
+            ms = time_steps(step)
+            flops = n * n * (n + 1) if name == "covariance" else n * n * (n - 1)
+            res[prec.name.lower()] = {"ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                                      "frob_rel": float(np.linalg.norm(e) / np.linalg.norm(ref)),
+                                      "max_rel": float(np.abs(e).max() / np.abs(ref).max())}
+            del got, e, ref
+        res["speedup_bf16x3_vs_fp32"] = res["bf16x3"]["tflops"] / res["fp32"]["tflops"]
+        stats[name] = res
+        for b in (dD, dMu, dSd, dS, dY, dR64):
+            ctx.free(b)
+    del cov, corr
+    out.update(stats)
+
+    # ---- matmulchain on identities: P = A.B, Q = C.D, R = P.Q
+    eye = np.eye(n, dtype=np.float32)
+    mats = [ctx.upload(eye) for _ in range(4)]
+    P, Q, R = (ctx.alloc(n * n * 4) for _ in range(3))
+    res = {}
+    for prec in (Precision.FP32, Precision.BF16X3):
+        plan = ctx.grouped_plan(prec, ctx.descs([
+            {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": mats[0], "lda": n, "B": mats[1], "ldb": n,
+             "C": P, "ldc": n},
+            {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": mats[2], "lda": n, "B": mats[3], "ldb": n,
+             "C": Q, "ldc": n}]))
+        ctx.workspace_reserve(ctx.workspace_query(prec, n, n, n))
+
+        def chain(prec=prec, plan=plan):
+            if prec == Precision.FP32:
+                ctx.gemm(prec, n, n, n, 1.0, mats[0], n, mats[1], n, 0.0, P, n)
+                ctx.gemm(prec, n, n, n, 1.0, mats[2], n, mats[3], n, 0.0, Q, n)
+            else:
+                ctx.grouped_run(plan)
+            ctx.gemm(prec, n, n, n, 1.0, P, n, Q, n, 0.0, R, n)
+        chain()
+        ctx.synchronize()
+        exact = bool(np.array_equal(ctx.download(R, (n, n)), eye))
+        g = None
+        if prec != Precision.FP32:
+            ctx.graph_begin()
+            chain()
+            g = ctx.graph_end()
+        ms = time_steps((lambda: ctx.graph_launch(g)) if g else chain)
+        res[prec.name.lower()] = {"ms_per_step": ms, "tflops": 6.0 * n ** 3 / (ms * 1e-3) / 1e12,
+                                  "identity_exact": exact,
+                                  "mode": "grouped P,Q + R in one CUDA graph" if g else "three launches"}
+        if g:
+            ctx.graph_destroy(g)
+        ctx.grouped_destroy(plan)
+    res["speedup_bf16x3_vs_fp32"] = res["bf16x3"]["tflops"] / res["fp32"]["tflops"]
+    out["matmulchain"] = res
+    for b in mats + [P, Q, R]:
+        ctx.free(b)
+    del eye
+
+    # ---- matrix-vector benchmarks at the suite runner's sizes
+    mv = {}
+    for name, m in (("atax", 4096), ("bicg", 16384), ("mvt", 16384), ("gesummv", 16384)):
+        rng = np.random.default_rng(11)
+        A = rng.uniform(-1, 1, (m, m)).astype(np.float32)
+        v1, v2 = (rng.uniform(-1, 1, m).astype(np.float32) for _ in range(2))
+        dA, d1, d2 = ctx.upload(A), ctx.upload(v1), ctx.upload(v2)
+        y1, y2 = ctx.upload(np.zeros(m, np.float32)), ctx.upload(np.zeros(m, np.float32))
+        dB = ctx.upload(A[::-1].copy()) if name == "gesummv" else None
+        a64 = A.astype(np.float64)
+        if name == "atax":
+            def step():
+                ctx.gemv(Op.N, m, m, 1.0, dA, m, d1, 0.0, y1)
+                ctx.gemv(Op.T, m, m, 1.0, dA, m, y1, 0.0, y2)
+            t = a64 @ v1.astype(np.float64)
+            refs, outs, passes = [a64.T @ t], [y2], 2
+        elif name == "bicg":
+            def step():
+                ctx.gemv_pair(m, m, dA, m, [(Op.T, 1.0, 0.0, d1, y1), (Op.N, 1.0, 0.0, d2, y2)])
+            refs, outs, passes = [a64.T @ v1.astype(np.float64), a64 @ v2.astype(np.float64)], [y1, y2], 1
+        elif name == "mvt":
+            def step():
+                ctx.gemv_pair(m, m, dA, m, [(Op.N, 1.0, 0.0, d1, y1), (Op.N, 1.0, 0.0, d2, y2)])
+            refs, outs, passes = [a64 @ v1.astype(np.float64), a64 @ v2.astype(np.float64)], [y1, y2], 1
+        else:
+            # tmp += A x; y = tmp + (y + B x): from zero tmp and y, the first call gives A x + B x
+            def step():
+                ctx.gesummv(m, m, 1.0, dA, m, dB, m, d1, 1.0, y1, y2)
+            refs = [a64 @ v1.astype(np.float64) + a64[::-1] @ v1.astype(np.float64)]
+            outs, passes = [y2], 2
+        step()
+        ctx.synchronize()
+        errs = [float(np.linalg.norm(ctx.download(o, (m,)).astype(np.float64) - r) / np.linalg.norm(r))
+                for o, r in zip(outs, refs)]
+        ms = time_steps(step, steps=max(args.steps, 20))
+        matrix_bytes = (2 if name == "gesummv" else 1) * m * m * 4
+        gbs = matrix_bytes / (ms * 1e-3) / 1e9
+        mv[name] = {"size": m, "us_per_call": ms * 1e3, "matrix_gbs": gbs,
+                    "frac_of_hbm": gbs / hbm if hbm else None, "matrix_passes": passes,
+                    "frob_rel_vs_fp64": max(errs)}
+        for b in (dA, d1, d2, y1, y2) + ((dB,) if dB is not None else ()):
+            ctx.free(b)
+        del A, a64
+    out["matrix_vector"] = mv
     return out
 
 
@@ -613,6 +800,8 @@ def main() -> None:
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-GEMM workload")
     ap.add_argument("--grouped-count", type=int, default=512)
     ap.add_argument("--no-family", action="store_true", help="skip the 2mm/3mm/syrk/syr2k section")
+    ap.add_argument("--no-neighbours", action="store_true",
+                    help="skip covariance/correlation/matmulchain/matrix-vector section")
     ap.add_argument("--forms", default="fp32,bf16x3,tf32x3,bf16x6,tf32,fp8", help="forms to time (comma list)")
     ap.add_argument("--tile-config", type=int, default=None, help="force this tile configuration (no autotuning)")
     ap.add_argument("--family-size", type=int, default=4096)
@@ -663,7 +852,8 @@ def main() -> None:
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
-                    peaks=res["peak_kind"], grouped=res["grouped"], family=res["family"])
+                    peaks=res["peak_kind"], grouped=res["grouped"], family=res["family"],
+                    neighbours=res["neighbours"])
         print(json.dumps(line))
     dist.close()
 

@@ -2,6 +2,7 @@
 
     python sycl-bench_gb300/build.py            # library + executables
     python sycl-bench_gb300/build.py --lib      # library only
+    python sycl-bench_gb300/build.py --install PREFIX   # + PREFIX/bin/benchmarks/<name> links
 
 Outputs (git-ignored):
     sycl-bench_gb300/lib/libgbpoly.so
@@ -125,16 +126,41 @@ def build_executables() -> list[Path]:
     return outs
 
 
+def install(prefix: Path) -> list[Path]:
+    """Link the built executables into <prefix>/bin/benchmarks/<name>, the
+    layout the reference's suite runner walks (CMakeLists.txt:170 installs
+    there; bin/run-suite runs every executable it finds in the benchmarks
+    directory beside itself).  Links resolve to this tree, so each executable
+    still finds lib/libgbpoly.so through its $ORIGIN run path."""
+    dest = Path(prefix) / "bin" / "benchmarks"
+    dest.mkdir(parents=True, exist_ok=True)
+    out = []
+    for _, name in BENCHMARKS:
+        src = BIN_DIR / name
+        if not src.exists():
+            continue
+        link = dest / name
+        if link.is_symlink() or link.exists():
+            link.unlink()
+        link.symlink_to(src)
+        out.append(link)
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--lib", action="store_true", help="library only")
     ap.add_argument("-v", "--verbose", action="store_true", help="ptxas resource usage")
+    ap.add_argument("--install", metavar="PREFIX", help="also link the executables into PREFIX/bin/benchmarks/")
     args = ap.parse_args()
     lib = build_lib(verbose=args.verbose)
     print(lib)
     if not args.lib and (POLY / "gemm.cpp").exists():
         for p in build_executables():
             print(p)
+        if args.install:
+            for p in install(Path(args.install)):
+                print(p)
 
 
 if __name__ == "__main__":

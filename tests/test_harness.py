@@ -158,3 +158,27 @@ def test_alpha_beta_variant_name():
     out = run("syrk", "--size=16", "--device=cpu", "--num-runs=1", "--alpha=32412", "--beta=2123").stdout
     assert "Results for Polybench_Syrk_ab32412_2123" in out
     assert "Verification: PASS" in out
+
+
+def test_install_layout_runs_like_the_suite_runner(tmp_path):
+    """build.py --install puts every executable under <prefix>/bin/benchmarks/,
+    where the reference's bin/run-suite looks; each one run the way the runner
+    invokes it (its default options with the cpu profile) exits 0 and appends
+    its rows to the shared CSV."""
+    import os
+    import sys
+    sys.path.insert(0, str(ROOT / "sycl-bench_gb300"))
+    import build
+    links = build.install(tmp_path)
+    bench_dir = tmp_path / "bin" / "benchmarks"
+    names = sorted(p.name for p in bench_dir.iterdir())
+    assert names == sorted(list(BENCHES) + list(FLOAT_ONLY)) and len(links) == len(names)
+    csv = tmp_path / "sycl-bench.csv"
+    for name in names:
+        exe = os.path.realpath(bench_dir / name)
+        r = subprocess.run([exe, "--device=cpu", "--num-runs=2", f"--output={csv}", "--size=32", "--local=256"],
+                           capture_output=True, text=True, timeout=300, cwd=tmp_path)
+        assert r.returncode == 0, (name, r.stderr)
+    rows = [ln for ln in csv.read_text().splitlines() if ln and not ln.startswith("#")]
+    assert all(",PASS," in ln for ln in rows), rows
+    assert {ln.split(",")[0] for ln in rows} >= set(BENCHES.values()) | set(FLOAT_ONLY.values())
