@@ -221,62 +221,75 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
   if(!ok) return;
 
   // --------------------------------------------------------------- epilogue
-  if(mirror) {  // C[n][m] from the product element (m, n): the tile's transpose, strictly above the diagonal
+  // C = alpha * acc + beta * C, four rows (then, below the diagonal of a
+  // symmetric product, four transposed rows) at a time: the 32 C values of a
+  // group are loaded before the group's first store.  A load cannot move above
+  // a store that may alias it, so interleaving them per element would
+  // serialise one memory round trip per element.
+  constexpr bool kVecCols = !B_KMAJ && !DUAL;
+  const bool vec_ok = kVecCols && ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+  int rm[8], cn[8];  // owned rows (m) and columns (n)
 #pragma unroll
-    for(int j = 0; j < 8; ++j) {
-      const int n = n0 + owned_index<B_KMAJ || DUAL>(tn, j);
-      if(n >= N) continue;
-      float* crow = C + static_cast<int64_t>(n) * ldc;
+  for(int i = 0; i < 8; ++i) rm[i] = m0 + owned_index<A_KMAJ || DUAL>(tm, i);
 #pragma unroll
-      for(int i = 0; i < 8; ++i) {
-        const int m = m0 + owned_index<A_KMAJ || DUAL>(tm, i);
-        if(m < M) {
-          const float v = alpha * acc[i][j];
-          crow[m] = (beta != 0.f) ? fmaf(beta, crow[m], v) : v;
+  for(int j = 0; j < 8; ++j) cn[j] = n0 + owned_index<B_KMAJ || DUAL>(tn, j);
+  const bool read_c = beta != 0.f;
+#pragma unroll
+  for(int g = 0; g < 8; g += 4) {
+    float cv[4][8];
+#pragma unroll
+    for(int r = 0; r < 4; ++r) {
+      const int i = g + r;
+      const float* crow = C + static_cast<int64_t>(rm[i]) * ldc;
+#pragma unroll
+      for(int h = 0; h < 2; ++h) {
+        if(read_c && vec_ok && rm[i] < M && cn[4 * h] + 3 < N) {
+          const float4 c = *reinterpret_cast<const float4*>(crow + cn[4 * h]);
+          cv[r][4 * h + 0] = c.x, cv[r][4 * h + 1] = c.y, cv[r][4 * h + 2] = c.z, cv[r][4 * h + 3] = c.w;
+        } else {
+#pragma unroll
+          for(int q = 0; q < 4; ++q)
+            cv[r][4 * h + q] = (read_c && rm[i] < M && cn[4 * h + q] < N) ? crow[cn[4 * h + q]] : 0.f;
+        }
+      }
+    }
+#pragma unroll
+    for(int r = 0; r < 4; ++r) {
+      const int i = g + r;
+      if(rm[i] >= M) continue;
+      float* crow = C + static_cast<int64_t>(rm[i]) * ldc;
+#pragma unroll
+      for(int h = 0; h < 2; ++h) {
+        float o[4];
+#pragma unroll
+        for(int q = 0; q < 4; ++q) o[q] = fmaf(beta, cv[r][4 * h + q], alpha * acc[i][4 * h + q]);
+        if(vec_ok && cn[4 * h] + 3 < N) {
+          *reinterpret_cast<float4*>(crow + cn[4 * h]) = make_float4(o[0], o[1], o[2], o[3]);
+        } else {
+#pragma unroll
+          for(int q = 0; q < 4; ++q)
+            if(cn[4 * h + q] < N) crow[cn[4 * h + q]] = o[q];
         }
       }
     }
   }
-  constexpr bool kVecCols = !B_KMAJ && !DUAL;
-  const bool vec_ok = kVecCols && ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+  if(mirror) {  // C[n][m] from the product element (m, n): the tile's transpose, strictly above the diagonal
 #pragma unroll
-  for(int i = 0; i < 8; ++i) {
-    const int m = m0 + owned_index<A_KMAJ || DUAL>(tm, i);
-    if(m >= M) continue;
-    float* crow = C + static_cast<int64_t>(m) * ldc;
-    if(vec_ok) {
+    for(int g = 0; g < 8; g += 4) {
+      float mv[4][8];
 #pragma unroll
-      for(int h = 0; h < 2; ++h) {
-        const int n = n0 + h * 64 + 4 * tn;
-        if(n + 3 < N) {
-          float4 out = make_float4(alpha * acc[i][4 * h + 0], alpha * acc[i][4 * h + 1], alpha * acc[i][4 * h + 2],
-              alpha * acc[i][4 * h + 3]);
-          if(beta != 0.f) {
-            const float4 c = *reinterpret_cast<const float4*>(crow + n);
-            out.x = fmaf(beta, c.x, out.x);
-            out.y = fmaf(beta, c.y, out.y);
-            out.z = fmaf(beta, c.z, out.z);
-            out.w = fmaf(beta, c.w, out.w);
-          }
-          *reinterpret_cast<float4*>(crow + n) = out;
-          continue;
-        }
+      for(int r = 0; r < 4; ++r)
 #pragma unroll
-        for(int q = 0; q < 4; ++q) {
-          if(n + q < N) {
-            const float v = alpha * acc[i][4 * h + q];
-            crow[n + q] = (beta != 0.f) ? fmaf(beta, crow[n + q], v) : v;
-          }
-        }
-      }
-    } else {
+        for(int i = 0; i < 8; ++i)
+          mv[r][i] = (read_c && cn[g + r] < N && rm[i] < M) ? C[static_cast<int64_t>(cn[g + r]) * ldc + rm[i]] : 0.f;
 #pragma unroll
-      for(int j = 0; j < 8; ++j) {
-        const int n = n0 + owned_index<B_KMAJ || DUAL>(tn, j);
-        if(n < N) {
-          const float v = alpha * acc[i][j];
-          crow[n] = (beta != 0.f) ? fmaf(beta, crow[n], v) : v;
-        }
+      for(int r = 0; r < 4; ++r) {
+        const int j = g + r;
+        if(cn[j] >= N) continue;
+        float* crow = C + static_cast<int64_t>(cn[j]) * ldc;
+#pragma unroll
+        for(int i = 0; i < 8; ++i)
+          if(rm[i] < M) crow[rm[i]] = fmaf(beta, mv[r][i], alpha * acc[i][j]);
       }
     }
   }
