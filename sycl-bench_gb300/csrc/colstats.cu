@@ -7,7 +7,7 @@
 // correlation.cpp:111-142).  Here a column reduction is two launches:
 //   * partial pass: a CTA of 8 warps owns 32 adjacent columns and one chunk
 //     of rows; lane j of every warp reads column j (a warp reads 128
-//     contiguous bytes of a row), each thread keeps four independent loads
+//     contiguous bytes of a row), each thread keeps eight independent loads
 //     in flight, and the 8 warps are combined in shared memory into one
 //     partial sum per (chunk, column);
 //   * final pass: one thread per column adds its chunks' partials in chunk
@@ -25,34 +25,39 @@ constexpr int kColsPerBlock = 32;
 constexpr int kWarps = 8;
 
 // sum over rows [r0, r1) of f(X[r][j]) for this thread's column j, rows
-// warp, warp + 8, ... of the chunk; four loads in flight.
+// warp, warp + 8, ... of the chunk; eight loads in flight.
 template <bool CENTERED>
 __device__ __forceinline__ float column_chunk_sum(const float* __restrict__ col, int64_t ldx, int r0, int r1, int warp,
     float m) {
-  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  constexpr int kLoads = 8;
+  float a[kLoads];
+#pragma unroll
+  for(int k = 0; k < kLoads; ++k) a[k] = 0.f;
   int r = r0 + warp;
-  for(; r + 3 * kWarps < r1; r += 4 * kWarps) {
-    float v0 = col[int64_t(r) * ldx];
-    float v1 = col[int64_t(r + kWarps) * ldx];
-    float v2 = col[int64_t(r + 2 * kWarps) * ldx];
-    float v3 = col[int64_t(r + 3 * kWarps) * ldx];
-    if constexpr(CENTERED) {
-      v0 -= m, v1 -= m, v2 -= m, v3 -= m;
-      a0 = fmaf(v0, v0, a0), a1 = fmaf(v1, v1, a1), a2 = fmaf(v2, v2, a2), a3 = fmaf(v3, v3, a3);
-    } else {
-      a0 += v0, a1 += v1, a2 += v2, a3 += v3;
+  for(; r + (kLoads - 1) * kWarps < r1; r += kLoads * kWarps) {
+    float v[kLoads];
+#pragma unroll
+    for(int k = 0; k < kLoads; ++k) v[k] = col[int64_t(r + k * kWarps) * ldx];
+#pragma unroll
+    for(int k = 0; k < kLoads; ++k) {
+      if constexpr(CENTERED) {
+        const float c = v[k] - m;
+        a[k] = fmaf(c, c, a[k]);
+      } else {
+        a[k] += v[k];
+      }
     }
   }
   for(; r < r1; r += kWarps) {
     float v = col[int64_t(r) * ldx];
     if constexpr(CENTERED) {
       v -= m;
-      a0 = fmaf(v, v, a0);
+      a[0] = fmaf(v, v, a[0]);
     } else {
-      a0 += v;
+      a[0] += v;
     }
   }
-  return (a0 + a1) + (a2 + a3);
+  return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
 }
 
 // partial[chunk][j] = sum over the chunk's rows of X[r][j] (or (X[r][j] - mean[j])^2).
@@ -102,10 +107,23 @@ __global__ void __launch_bounds__(256) center_columns_kernel(const float* X, int
   const float m = mean[j];
   const float sd = SCALED ? stddev[j] : 1.f;
   const int r0 = blockIdx.y * rows_per_block, r1 = min(rows, r0 + rows_per_block);
-  for(int r = r0 + (threadIdx.x >> 5); r < r1; r += 8) {
-    float v = X[int64_t(r) * ldx + j] - m;
-    if constexpr(SCALED) v = (v / scale_div) / sd;
-    Y[int64_t(r) * ldy + j] = v;
+  // eight rows per batch, all loaded before the first store (Y may be X, so a
+  // load could not otherwise move above the previous store)
+  constexpr int kBatch = 8;
+  for(int rb = r0 + (threadIdx.x >> 5); rb < r1; rb += 8 * kBatch) {
+    float v[kBatch];
+#pragma unroll
+    for(int k = 0; k < kBatch; ++k) {
+      const int r = rb + 8 * k;
+      v[k] = r < r1 ? X[int64_t(r) * ldx + j] : 0.f;
+    }
+#pragma unroll
+    for(int k = 0; k < kBatch; ++k) {
+      const int r = rb + 8 * k;
+      float y = v[k] - m;
+      if constexpr(SCALED) y = (y / scale_div) / sd;
+      if(r < r1) Y[int64_t(r) * ldy + j] = y;
+    }
   }
 }
 
