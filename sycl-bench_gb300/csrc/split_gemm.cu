@@ -53,10 +53,26 @@ namespace {
 
 enum class Elem { BF16, TF32, E4M3 };
 
-template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128>
+// Instruction descriptor of an M x N MMA of element type E (FP32 accumulation).
+template <Elem E, int M, int N>
+constexpr uint32_t idesc_of() {
+  if constexpr(E == Elem::E4M3)
+    return umma::InstrDescE4M3<M, N>::value;
+  else
+    return umma::InstrDesc<M, N, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
+}
+
+// CG_ = 2: a CTA pair (cluster of two) computes a (256 x BN) tile with
+// cta_group::2 MMAs: each CTA holds 128 rows of the A tile and BN/2 rows of
+// the B tile in its shared memory, and 128 rows x BN columns of the
+// accumulator in its TMEM.
+template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128, int CG_ = 1>
 struct Form {
   static constexpr Elem elem = E;
-  static constexpr int terms = TERMS, nprod = NPROD, BM = 128, BN = BN_, STAGES = STAGES_;
+  static constexpr int CG = CG_;
+  static constexpr int terms = TERMS, nprod = NPROD, BN = BN_, STAGES = STAGES_;
+  static constexpr int BM_CTA = 128, BM = BM_CTA * CG;   // rows per CTA; rows of a (pair) tile
+  static constexpr int BN_CTA = BN / CG;                 // B rows staged per CTA
   static constexpr int ROW = ROW_;                       // bytes of K per smem row (= swizzle width)
   static constexpr int esz = E == Elem::BF16 ? 2 : (E == Elem::TF32 ? 4 : 1);
   static constexpr int BK = ROW / esz;                   // K elements per stage
@@ -64,8 +80,9 @@ struct Form {
   // E4M3 operands carry one scale per 128 x 128 block: a stage (128 bytes of
   // K) is exactly one block along K, so each TMEM chunk has one scale.
   static constexpr bool scaled = E == Elem::E4M3;
-  static constexpr int A_TILE = BM * ROW, B_TILE = BN * ROW;
-  static constexpr int STAGE = TERMS * (A_TILE + B_TILE);
+  static constexpr int A_TILE = BM_CTA * ROW, B_TILE = BN_CTA * ROW;
+  static constexpr int STAGE = TERMS * (A_TILE + B_TILE);  // bytes per stage in each CTA
+  static constexpr int STAGE_TX = CG * STAGE;              // bytes a stage's barrier waits for (both CTAs)
   static constexpr int EPI_STAGE = 8 * 32 * 33 * 4;  // epilogue staging, one 32x33 fp32 tile per warp
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + EPI_STAGE;
   // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
@@ -75,12 +92,15 @@ struct Form {
   static constexpr int CH = 128 / ROW;
   static constexpr uint32_t TMEM_COLS = 2 * BN;
   static constexpr int HALF = BN / 2;  // columns per epilogue warp
+  // Square tiles whose epilogue also fits the mirrored stores of symmetric
+  // updates in registers (lower triangle of tiles).
+  static constexpr bool MIRROR = BM == BN && HALF <= 64;
   static constexpr int THREADS = 384;  // warpgroup 0: producer, MMA; warpgroups 1-2: epilogue
   static constexpr uint32_t REGS_CTRL = 56, REGS_EPI = 208;
-  static constexpr uint32_t IDESC =
-      E == Elem::E4M3 ? umma::InstrDescE4M3<BM, BN>::value
-                      : umma::InstrDesc<BM, BN, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
+  static constexpr uint32_t IDESC = idesc_of<E, BM, BN>();
   static_assert(!scaled || (ROW == 128 && CH == 1), "one scale block per chunk");
+  static_assert(CG == 1 || (CG == 2 && !scaled && BN % 32 == 0), "CTA pairs: BF16 and TF32 forms");
+  static_assert(STAGE_TX == CG * STAGE, "pair stage bytes");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert(TMEM_COLS <= 512, "tensor memory");
 };
@@ -99,6 +119,16 @@ using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
 using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
 using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 2, 64>;
 using FormFP8 = Form<Elem::E4M3, 1, 1, 128, 6>;
+// CTA-pair configurations (cluster of 2, 256 x 256 tiles)
+using FormTF32_p = Form<Elem::TF32, 1, 1, 256, 6, 128, 2>;
+using FormBF16x3_p = Form<Elem::BF16, 2, 3, 256, 3, 128, 2>;
+using FormTF32x3_p = Form<Elem::TF32, 2, 3, 256, 3, 128, 2>;
+using FormBF16x6_p = Form<Elem::BF16, 3, 6, 256, 2, 128, 2>;
+// CTA pairs with 64-byte rows: more, shorter stages
+using FormTF32_q = Form<Elem::TF32, 1, 1, 256, 12, 64, 2>;
+using FormBF16x3_q = Form<Elem::BF16, 2, 3, 256, 6, 64, 2>;
+using FormTF32x3_q = Form<Elem::TF32, 2, 3, 256, 6, 64, 2>;
+using FormBF16x6_q = Form<Elem::BF16, 3, 6, 256, 4, 64, 2>;
 
 // Term indices of product p: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 ? 1 : (p == 4 ? 1 : (p == 5 ? 2 : 0)); }
@@ -382,6 +412,12 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = sched.count();
+  // CTA pairs: tiles are walked per cluster; rank 0 issues the MMAs and owns
+  // the stage barriers, both CTAs load their halves and run the epilogue on
+  // their 128 rows.
+  const uint32_t rank = F::CG == 2 ? cluster_ctarank() : 0u;
+  const int first_tile = F::CG == 2 ? int(cluster_id_x()) : int(blockIdx.x);
+  const int tile_step = F::CG == 2 ? int(cluster_count_x()) : int(gridDim.x);
 
   if(threadIdx.x == 0) {
     for(int s = 0; s < F::STAGES; ++s) {
@@ -390,17 +426,25 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     }
     for(int b = 0; b < 2; ++b) {
       mbar_init(&chunk_full[b], 1);
-      mbar_init(&chunk_empty[b], 8);  // one arrival per epilogue warp
+      mbar_init(&chunk_empty[b], 8 * F::CG);  // one arrival per epilogue warp of the pair
     }
     mbar_init(drain, 1);
     fence_mbar_init();
   }
   if(warp == 1) {
-    umma::tmem_alloc(tmem_slot, F::TMEM_COLS);
-    umma::tmem_relinquish();
+    if constexpr(F::CG == 2) {
+      umma::tmem_alloc_pair(tmem_slot, F::TMEM_COLS);
+      umma::tmem_relinquish_pair();
+    } else {
+      umma::tmem_alloc(tmem_slot, F::TMEM_COLS);
+      umma::tmem_relinquish();
+    }
   }
   umma::fence_before_sync();
-  __syncthreads();
+  if constexpr(F::CG == 2)
+    cluster_sync();  // both CTAs' barriers initialised before any remote arrival
+  else
+    __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
@@ -410,9 +454,9 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       // ---------------------------------------------------------- producer
       int g = 0;  // global stage iteration across tiles
       bool ok = true;
-      for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+      for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
         const TileInfo ti = sched.tile(tile);
-        const int m0 = ti.m0, n0 = ti.n0, npair = ti.npair;
+        const int m0 = ti.m0 + int(rank) * F::BM_CTA, n0 = ti.n0 + int(rank) * F::BN_CTA, npair = ti.npair;
         const int iters = (ti.Kp / F::BK) * npair;
         for(int it = 0; it < iters; ++it, ++g) {
           const int s = g % F::STAGES;
@@ -423,22 +467,36 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           const ProductMaps& pm = ti.maps[it % npair];
           const int k0 = (it / npair) * F::BK;
           char* st = smem + s * F::STAGE;
-          mbar_arrive_expect_tx(&full[s], F::STAGE);
+          if constexpr(F::CG == 2) {
+            // both CTAs' boxes complete on the first CTA's barrier, which expects the pair's bytes
+            const uint32_t bar = cluster_map(&full[s], 0);
+            if(rank == 0) mbar_arrive_expect_tx(&full[s], F::STAGE_TX);
 #pragma unroll
-          for(int t = 0; t < F::terms; ++t) {
-            tma_load_2d(st + t * F::A_TILE, &pm.l[t], &full[s], k0, m0);
-            tma_load_2d(st + F::terms * F::A_TILE + t * F::B_TILE, &pm.r[t], &full[s], k0, n0);
+            for(int t = 0; t < F::terms; ++t) {
+              tma_load_2d_pair(st + t * F::A_TILE, &pm.l[t], bar, k0, m0);
+              tma_load_2d_pair(st + F::terms * F::A_TILE + t * F::B_TILE, &pm.r[t], bar, k0, n0);
+            }
+          } else {
+            mbar_arrive_expect_tx(&full[s], F::STAGE);
+#pragma unroll
+            for(int t = 0; t < F::terms; ++t) {
+              tma_load_2d(st + t * F::A_TILE, &pm.l[t], &full[s], k0, m0);
+              tma_load_2d(st + F::terms * F::A_TILE + t * F::B_TILE, &pm.r[t], &full[s], k0, n0);
+            }
           }
         }
       }
-      // do not leave while copies into this CTA's shared memory are in flight
-      for(int h = max(0, g - F::STAGES); h < g; ++h)
-        if(!mbar_wait(&full[h % F::STAGES], (h / F::STAGES) & 1, err, kDevErrDrainWait)) break;
-    } else if(warp == 1 && lane == 0) {
+      // do not leave while copies into shared memory are in flight: the
+      // first CTA's barriers count the copies of both CTAs of a pair, and the
+      // second CTA leaves only after the pair's final cluster barrier
+      if(rank == 0)
+        for(int h = max(0, g - F::STAGES); h < g; ++h)
+          if(!mbar_wait(&full[h % F::STAGES], (h / F::STAGES) & 1, err, kDevErrDrainWait)) break;
+    } else if(warp == 1 && lane == 0 && rank == 0) {
       // ------------------------------------------------------- MMA issue
       int g = 0, chunk = 0;
       bool ok = true;
-      for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+      for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
         const TileInfo ti = sched.tile(tile);
         const int iters = (ti.Kp / F::BK) * ti.npair;
         for(int it = 0; it < iters && ok; ++it, ++g) {
@@ -472,21 +530,39 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             const uint64_t da = umma::desc_k<F::ROW>(a_base + prod_a(p) * F::A_TILE + off);
             const uint64_t db = umma::desc_k<F::ROW>(b_base + prod_b(p) * F::B_TILE + off);
             const uint32_t acc = (it % F::CH != 0 || q > 0) ? 1u : 0u;
-            if constexpr(F::elem == Elem::BF16)
+            if constexpr(F::CG == 2) {
+              if constexpr(F::elem == Elem::BF16)
+                umma::mma_f16_pair(d, da, db, F::IDESC, acc);
+              else
+                umma::mma_tf32_pair(d, da, db, F::IDESC, acc);
+            } else if constexpr(F::elem == Elem::BF16) {
               umma::mma_f16(d, da, db, F::IDESC, acc);
-            else if constexpr(F::elem == Elem::TF32)
+            } else if constexpr(F::elem == Elem::TF32) {
               umma::mma_tf32(d, da, db, F::IDESC, acc);
-            else
+            } else {
               umma::mma_f8(d, da, db, F::IDESC, acc);
+            }
           }
-          umma::commit(&empty[s]);  // stage s is free once these MMAs have read it
+          // stage s is free once these MMAs have read it (in both CTAs of a pair)
+          if constexpr(F::CG == 2)
+            umma::commit_pair(&empty[s], 0x3);
+          else
+            umma::commit(&empty[s]);
           if(it % F::CH == F::CH - 1 || it == iters - 1) {
-            umma::commit(&chunk_full[b]);  // chunk complete in TMEM buffer b
+            // chunk complete in TMEM buffer b
+            if constexpr(F::CG == 2)
+              umma::commit_pair(&chunk_full[b], 0x3);
+            else
+              umma::commit(&chunk_full[b]);
             ++chunk;
           }
         }
       }
-      umma::commit(drain);  // every MMA issued by this thread has completed
+      // every MMA issued by this thread has completed
+      if constexpr(F::CG == 2)
+        umma::commit_pair(drain, 0x1);
+      else
+        umma::commit(drain);
       mbar_wait(drain, 0, err, kDevErrDrainWait);
     }
   } else {
@@ -497,7 +573,10 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     float acc[F::HALF];
     int chunk = 0;
     bool ok = true;
-    for(int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    // chunk buffers are released on the first CTA's barrier (MMAs are issued there)
+    const uint32_t chunk_empty_pair[2] = {F::CG == 2 ? cluster_map(&chunk_empty[0], 0) : 0u,
+        F::CG == 2 ? cluster_map(&chunk_empty[1], 0) : 0u};
+    for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
       const TileInfo ti = sched.tile(tile);
       const int M = ti.M, N = ti.N;
       const float alpha = ti.alpha, beta = ti.beta;
@@ -532,14 +611,19 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
         umma::fence_before_sync();
         __syncwarp();
-        if(lane == 0) mbar_arrive(&chunk_empty[b]);
+        if(lane == 0) {
+          if constexpr(F::CG == 2)
+            mbar_arrive_cluster(b ? chunk_empty_pair[1] : chunk_empty_pair[0]);
+          else
+            mbar_arrive(&chunk_empty[b]);
+        }
       }
       if(!ok) continue;
       // Write C through a per-warp 32 x 32 staging tile: each lane holds one
       // row of the block, the stores go out one 128-byte row segment per
       // instruction (coalesced for any ldc and alignment).
       float(*stage)[33] = epi_stage + (warp - 4) * 32;
-      const int row0 = ti.m0 + 32 * q;
+      const int row0 = ti.m0 + int(rank) * F::BM_CTA + 32 * q;
 #pragma unroll
       for(int j = 0; j < F::HALF / 32; ++j) {
 #pragma unroll
@@ -556,7 +640,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           for(int r = 0; r < 32; ++r)
             if(r < rows) col[int64_t(r) * ldc] = fmaf(beta, cv[r], alpha * stage[r][lane]);
         }
-        if constexpr(F::BM == F::BN) {
+        if constexpr(F::MIRROR) {
           if(ti.mirror) {
           // transpose: C[n0 + 32j + r][row0 + lane] from the product element (row0 + lane, n0 + 32j + r)
           const int mrow0 = nbase + 32 * j, mcol = row0 + lane;
@@ -582,10 +666,20 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   }
 
   umma::fence_before_sync();
-  __syncthreads();
-  if(warp == 1) {
-    umma::fence_after_sync();
-    umma::tmem_dealloc(tmem, F::TMEM_COLS);
+  if constexpr(F::CG == 2) {
+    // neither CTA leaves (or frees TMEM) while the pair's MMAs, copies or
+    // barrier arrivals may still target it
+    cluster_sync();
+    if(warp == 1) {
+      umma::fence_after_sync();
+      umma::tmem_dealloc_pair(tmem, F::TMEM_COLS);
+    }
+  } else {
+    __syncthreads();
+    if(warp == 1) {
+      umma::fence_after_sync();
+      umma::tmem_dealloc(tmem, F::TMEM_COLS);
+    }
   }
 }
 
@@ -617,11 +711,11 @@ gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, i
   const auto sw = F::ROW == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
   gbpoly_status st;
   for(int t = 0; t < F::terms; ++t) {
-    if((st = make_tmap_2d(ctx, &pm.l[t], dt, F::esz, left.base + t * left.stride, left_rows, Kp, Kp, F::BM, F::BK,
-            sw)) != GBPOLY_OK)
+    if((st = make_tmap_2d(ctx, &pm.l[t], dt, F::esz, left.base + t * left.stride, left_rows, Kp, Kp, F::BM_CTA,
+            F::BK, sw)) != GBPOLY_OK)
       return st;
-    if((st = make_tmap_2d(ctx, &pm.r[t], dt, F::esz, right.base + t * right.stride, right_rows, Kp, Kp, F::BN, F::BK,
-            sw)) != GBPOLY_OK)
+    if((st = make_tmap_2d(ctx, &pm.r[t], dt, F::esz, right.base + t * right.stride, right_rows, Kp, Kp, F::BN_CTA,
+            F::BK, sw)) != GBPOLY_OK)
       return st;
   }
   return GBPOLY_OK;
@@ -644,6 +738,33 @@ gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t tiles, c
     attr_set |= 1u << ctx->device;
   }
   if(tiles <= 0) return GBPOLY_OK;
+  if constexpr(F::CG == 2) {
+    // CTA pairs: a cluster of two per tile, as many clusters as fit at once
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(F::THREADS);
+    cfg.dynamicSmemBytes = F::SMEM;
+    cfg.stream = ctx->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    static int max_clusters[32] = {};
+    if(ctx->device >= 32 || max_clusters[ctx->device] == 0) {
+      cfg.gridDim = dim3(2 * (ctx->sm_count / 2));
+      int n = 0;
+      GBPOLY_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, split_gemm_kernel<F, S>, &cfg));
+      if(n <= 0) return fail(GBPOLY_ERR_UNSUPPORTED, "no CTA pair of this tensor-core configuration fits on the device");
+      if(ctx->device < 32) max_clusters[ctx->device] = n;
+    }
+    const int clusters = int(std::min<int64_t>(tiles, ctx->device < 32 ? max_clusters[ctx->device] : 1));
+    cfg.gridDim = dim3(2 * clusters);
+    ProfileScope prof(ctx, kernel_name);
+    GBPOLY_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_gemm_kernel<F, S>, sched, ctx->err_dev));
+    return GBPOLY_OK;
+  }
   const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
   ProfileScope prof(ctx, kernel_name);
   split_gemm_kernel<F, S><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(sched, ctx->err_dev);
@@ -706,7 +827,7 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
 
   SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
   int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
-  if(F::BM == F::BN && (same || a.dual) && a.M == a.N) {  // symmetric product: lower triangle of tiles
+  if(F::MIRROR && (same || a.dual) && a.M == a.N) {  // symmetric product: lower triangle of tiles
     const int64_t t = (a.M + F::BM - 1) / F::BM;
     sched.lower = true;
     tiles = t * (t + 1) / 2;
@@ -797,7 +918,7 @@ int tensor_config_count(gbpoly_precision prec) {
   case GBPOLY_PREC_TF32:
   case GBPOLY_PREC_BF16X3:
   case GBPOLY_PREC_TF32X3:
-  case GBPOLY_PREC_BF16X6: return 3;
+  case GBPOLY_PREC_BF16X6: return 5;  // configurations 3, 4: CTA pairs
   case GBPOLY_PREC_FP8: return 1;
   default: return 0;
   }
@@ -808,15 +929,23 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   case GBPOLY_PREC_TF32 * 8 + 0: return run_form<FormTF32>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 1: return run_form<FormTF32_b>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 2: return run_form<FormTF32_c>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 3: return run_form<FormTF32_p>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 4: return run_form<FormTF32_q>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form<FormBF16x3>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form<FormBF16x3_b>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form<FormBF16x3_c>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 3: return run_form<FormBF16x3_p>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 4: return run_form<FormBF16x3_q>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form<FormTF32x3>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form<FormTF32x3_b>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form<FormTF32x3_c>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 3: return run_form<FormTF32x3_p>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 4: return run_form<FormTF32x3_q>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form<FormBF16x6>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form<FormBF16x6_b>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form<FormBF16x6_c>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 3: return run_form<FormBF16x6_p>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form<FormBF16x6_q>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
@@ -846,8 +975,8 @@ gbpoly_status run_form_panel(gbpoly_ctx* ctx, const GemmF32Args& a, int64_t Mful
   return launch_tc_kernel<F>(ctx, sched, tiles, name);
 }
 
-// Square-tile (BM == BN == 128) configuration of each form: symmetric
-// updates need it to compute only the lower triangle of tiles.
+// Square-tile (128 x 128) configurations of each form: symmetric updates
+// need one to compute only the lower triangle of tiles.
 namespace {
 bool config_is_square(gbpoly_precision prec, int config) {
   switch(prec) {
@@ -876,15 +1005,23 @@ gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const G
   case GBPOLY_PREC_TF32 * 8 + 0: return run_form_panel<FormTF32>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 1: return run_form_panel<FormTF32_b>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 2: return run_form_panel<FormTF32_c>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 3: return run_form_panel<FormTF32_p>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 4: return run_form_panel<FormTF32_q>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form_panel<FormBF16x3>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form_panel<FormBF16x3_b>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form_panel<FormBF16x3_c>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 3: return run_form_panel<FormBF16x3_p>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 4: return run_form_panel<FormBF16x3_q>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form_panel<FormTF32x3>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form_panel<FormTF32x3_b>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form_panel<FormTF32x3_c>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 3: return run_form_panel<FormTF32x3_p>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 4: return run_form_panel<FormTF32x3_q>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form_panel<FormBF16x6>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form_panel<FormBF16x6_b>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form_panel<FormBF16x6_c>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 3: return run_form_panel<FormBF16x6_p>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form_panel<FormBF16x6_q>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);  // quantises both operands per panel
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }

@@ -1,0 +1,71 @@
+"""CTA-pair (cluster of two, cta_group::2) configurations of the tensor-core
+forms, through the C ABI: configurations 3 (128-byte rows) and 4 (64-byte
+rows, deeper pipeline) of tf32, bf16x3, tf32x3 and bf16x6 compute 256 x 256
+tiles with each CTA holding half of the A and B tiles.  Results against FP64 within each form's bound (the same bounds as
+the other configurations), on shapes that leave the second CTA of a pair
+beyond the last row, walk several tiles per cluster, and use one or many
+pipeline stages.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gbpoly import Op, Precision
+
+pytestmark = pytest.mark.gpu
+
+PAIR_CONFIGS = (3, 4)
+BOUND = {Precision.TF32: 1e-3, Precision.BF16X3: 2e-5, Precision.TF32X3: 5e-6, Precision.BF16X6: 5e-6}
+FORMS = list(BOUND)
+
+
+def run_pair(ctx, prec, A, B, C, alpha, beta, op_a=Op.N, op_b=Op.N, config=3):
+    M = A.shape[1] if op_a == Op.T else A.shape[0]
+    K = A.shape[0] if op_a == Op.T else A.shape[1]
+    N = B.shape[0] if op_b == Op.T else B.shape[1]
+    assert ctx.config_count(prec) > max(PAIR_CONFIGS)
+    ctx.config_set(prec, M, N, K, config)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.gemm(prec, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, dC, N, op_a=op_a, op_b=op_b)
+    ctx.synchronize()
+    out = ctx.download(dC, C.shape)
+    for b in (dA, dB, dC):
+        ctx.free(b)
+    ctx.config_set(prec, M, N, K, 0)
+    return out
+
+
+@pytest.mark.parametrize("M,N,K", [(256, 256, 64), (200, 130, 70), (520, 300, 333), (1024, 768, 1024),
+                                   (2304, 2048, 512)])
+@pytest.mark.parametrize("prec", FORMS, ids=lambda p: p.name.lower())
+@pytest.mark.parametrize("config", PAIR_CONFIGS)
+def test_pair_configuration_against_fp64(ctx, prec, M, N, K, config):
+    rng = np.random.default_rng(M + 7 * N + 13 * K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    C = rng.standard_normal((M, N)).astype(np.float32)
+    got = run_pair(ctx, prec, A, B, C, 1.25, -0.5, config=config)
+    ref = oracle.gemm_f64(A, B, C, 1.25, -0.5)
+    frob = oracle.error_norms(got, ref)[1]
+    assert frob < BOUND[prec], frob
+
+
+@pytest.mark.parametrize("ops", [(Op.T, Op.N), (Op.N, Op.T), (Op.T, Op.T)], ids=["TN", "NT", "TT"])
+@pytest.mark.parametrize("config", PAIR_CONFIGS)
+def test_pair_configuration_transposed_operands(ctx, ops, config):
+    M, N, K = 700, 600, 500
+    rng = np.random.default_rng(3)
+    A = rng.uniform(-1, 1, (K, M) if ops[0] == Op.T else (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (N, K) if ops[1] == Op.T else (K, N)).astype(np.float32)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    got = run_pair(ctx, Precision.BF16X3, A, B, C, 2.0, 0.25, op_a=ops[0], op_b=ops[1], config=config)
+    ref = oracle.gemm_f64(A, B, C, 2.0, 0.25, op_a=int(ops[0]), op_b=int(ops[1]))
+    assert oracle.error_norms(got, ref)[1] < BOUND[Precision.BF16X3]
+
+
+def test_pair_configuration_polybench_gemm_verifies(ctx):
+    n = 1024
+    A, B, C = oracle.init_gemm(n)
+    got = run_pair(ctx, Precision.BF16X3, A, B, C, 32412.0, 2123.0)
+    first, max_pd, nfail = oracle.verify(oracle.host_gemm(n), got)
+    assert first == -1, f"{nfail} elements over 0.05%, max {max_pd}"
