@@ -51,7 +51,7 @@ std::tuple<int, int, int, int> shape_bucket(gbpoly_precision prec, int64_t M, in
 
 int tuned_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K) {
   auto it = ctx->tuned.find(shape_bucket(prec, M, N, K));
-  return it == ctx->tuned.end() ? 0 : it->second;
+  return it == ctx->tuned.end() ? default_config(ctx, prec, M, N, K) : it->second;
 }
 
 }  // namespace gbpoly

@@ -142,6 +142,8 @@ gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const G
 int tensor_config_count(gbpoly_precision prec);
 gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, int config, const GemmF32Args& a);
 int tuned_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
+// Configuration used for a shape nobody tuned (split_gemm.cu).
+int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
 std::tuple<int, int, int, int> shape_bucket(gbpoly_precision prec, int64_t M, int64_t N, int64_t K);
 // Row-panel execution of a tensor-core contraction (host-buffer calls): the
 // plan fixes form and configuration for the full shape; each panel call

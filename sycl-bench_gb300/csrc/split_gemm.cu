@@ -92,9 +92,9 @@ struct Form {
   static constexpr int CH = 128 / ROW;
   static constexpr uint32_t TMEM_COLS = 2 * BN;
   static constexpr int HALF = BN / 2;  // columns per epilogue warp
-  // Square tiles whose epilogue also fits the mirrored stores of symmetric
-  // updates in registers (lower triangle of tiles).
-  static constexpr bool MIRROR = BM == BN && HALF <= 64;
+  // Square tiles: symmetric updates compute the lower triangle of tiles and
+  // mirror them.
+  static constexpr bool MIRROR = BM == BN;
   static constexpr int THREADS = 384;  // warpgroup 0: producer, MMA; warpgroups 1-2: epilogue
   static constexpr uint32_t REGS_CTRL = 56, REGS_EPI = 208;
   static constexpr uint32_t IDESC = idesc_of<E, BM, BN>();
@@ -633,12 +633,19 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         if(n < N) {
           const int rows = min(32, M - row0);
           float* col = ti.C + int64_t(row0) * ldc + n;
-          float cv[32];  // all 32 loads in flight before the first store
+          // a batch of loads in flight before its first store (16 while 128
+          // accumulator columns per warp are still live)
+          constexpr int kBatch = F::HALF > 64 ? 16 : 32;
 #pragma unroll
-          for(int r = 0; r < 32; ++r) cv[r] = (beta != 0.f && r < rows) ? col[int64_t(r) * ldc] : 0.f;
+          for(int r0 = 0; r0 < 32; r0 += kBatch) {
+            float cv[kBatch];
 #pragma unroll
-          for(int r = 0; r < 32; ++r)
-            if(r < rows) col[int64_t(r) * ldc] = fmaf(beta, cv[r], alpha * stage[r][lane]);
+            for(int r = 0; r < kBatch; ++r)
+              cv[r] = (beta != 0.f && r0 + r < rows) ? col[int64_t(r0 + r) * ldc] : 0.f;
+#pragma unroll
+            for(int r = 0; r < kBatch; ++r)
+              if(r0 + r < rows) col[int64_t(r0 + r) * ldc] = fmaf(beta, cv[r], alpha * stage[r0 + r][lane]);
+          }
         }
         if constexpr(F::MIRROR) {
           if(ti.mirror) {
@@ -647,14 +654,15 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           if(mcol < M) {
             const int rows = min(32, N - mrow0);
             float* col = ti.C + int64_t(mrow0) * ldc + mcol;
+            constexpr int kMBatch = F::HALF > 64 ? 8 : 16;  // loads in flight at a time
 #pragma unroll
-            for(int half = 0; half < 32; half += 16) {  // 16 loads in flight at a time
-              float cv[16];
+            for(int half = 0; half < 32; half += kMBatch) {
+              float cv[kMBatch];
 #pragma unroll
-              for(int r = 0; r < 16; ++r)
+              for(int r = 0; r < kMBatch; ++r)
                 cv[r] = (beta != 0.f && half + r < rows) ? col[int64_t(half + r) * ldc] : 0.f;
 #pragma unroll
-              for(int r = 0; r < 16; ++r)
+              for(int r = 0; r < kMBatch; ++r)
                 if(half + r < rows) col[int64_t(half + r) * ldc] = fmaf(beta, cv[r], alpha * stage[lane][half + r]);
             }
           }
@@ -975,21 +983,38 @@ gbpoly_status run_form_panel(gbpoly_ctx* ctx, const GemmF32Args& a, int64_t Mful
   return launch_tc_kernel<F>(ctx, sched, tiles, name);
 }
 
-// Square-tile (128 x 128) configurations of each form: symmetric updates
-// need one to compute only the lower triangle of tiles.
+// Square-tile configurations of each form (128 x 128, or 256 x 256 for CTA
+// pairs): symmetric updates need one to compute only the lower triangle of
+// tiles.
 namespace {
 bool config_is_square(gbpoly_precision prec, int config) {
   switch(prec) {
   case GBPOLY_PREC_TF32:
   case GBPOLY_PREC_BF16X3:
-  case GBPOLY_PREC_TF32X3: return config == 2;
-  case GBPOLY_PREC_BF16X6: return config == 0 || config == 1;
+  case GBPOLY_PREC_TF32X3: return config == 2 || config == 3 || config == 4;
+  case GBPOLY_PREC_BF16X6: return config == 0 || config == 1 || config == 3 || config == 4;
   case GBPOLY_PREC_FP8: return true;
   default: return false;
   }
 }
-int square_config(gbpoly_precision prec) { return prec == GBPOLY_PREC_BF16X6 ? 1 : (prec == GBPOLY_PREC_FP8 ? 0 : 2); }
+// CTA pairs when their 256 x 256 tiles give every SM pair at least one tile.
+bool pairs_fill(gbpoly_ctx* ctx, int64_t pair_tiles) { return pair_tiles >= std::max(1, ctx->sm_count / 2); }
+int square_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N) {
+  if(prec == GBPOLY_PREC_FP8) return 0;
+  const int64_t t = (N + 255) / 256;
+  if(pairs_fill(ctx, t * (t + 1) / 2)) return 3;
+  return prec == GBPOLY_PREC_BF16X6 ? 1 : 2;
+}
 }  // namespace
+
+// Configuration of an untuned shape: CTA pairs (256 x 256 tiles) when they
+// fill the device, else the 1-CTA configuration with the most tiles.
+int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t) {
+  if(prec == GBPOLY_PREC_FP8 || tensor_config_count(prec) <= 3) return 0;
+  if(pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256))) return 3;
+  // 128 x 128 tiles: configuration 2 (0 for bf16x6, whose configuration 0 is 128 x 128)
+  return prec == GBPOLY_PREC_BF16X6 ? 0 : 2;
+}
 
 gbpoly_status tensor_plan(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op, gbpoly_op, int64_t M, int64_t N,
     int64_t K, TensorPlan* plan) {
@@ -1030,7 +1055,7 @@ gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const G
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a) {
   int config = tuned_config(ctx, prec, a.M, a.N, a.K);
   const bool symmetric = (same_operand(a) || a.dual) && a.M == a.N;
-  if(symmetric && !config_is_square(prec, config)) config = square_config(prec);
+  if(symmetric && !config_is_square(prec, config)) config = square_config(ctx, prec, a.N);
   return launch_gemm_tensor_config(ctx, prec, config, a);
 }
 

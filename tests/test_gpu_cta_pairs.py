@@ -69,3 +69,32 @@ def test_pair_configuration_polybench_gemm_verifies(ctx):
     got = run_pair(ctx, Precision.BF16X3, A, B, C, 32412.0, 2123.0)
     first, max_pd, nfail = oracle.verify(oracle.host_gemm(n), got)
     assert first == -1, f"{nfail} elements over 0.05%, max {max_pd}"
+
+
+@pytest.mark.parametrize("config", PAIR_CONFIGS)
+@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.BF16X6], ids=lambda p: p.name.lower())
+def test_pair_configuration_symmetric_updates(ctx, prec, config):
+    # syrk and syr2k on 256 x 256 pair tiles: lower triangle of tiles, the
+    # tiles below the diagonal also store their transpose (beta on a
+    # non-symmetric C, so a wrong mirror shows)
+    n, k = 1000, 300
+    rng = np.random.default_rng(config)
+    A = rng.uniform(-1, 1, (n, k)).astype(np.float32)
+    B = rng.uniform(-1, 1, (n, k)).astype(np.float32)
+    C = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    dA, dB = ctx.upload(A), ctx.upload(B)
+    ctx.config_set(prec, n, n, k, config)
+    for name in ("syrk", "syr2k"):
+        dC = ctx.upload(C)
+        if name == "syrk":
+            ctx.syrk(prec, n, k, 1.5, dA, k, -0.5, dC, n)
+            ref = oracle.gemm_f64(A, A, C, 1.5, -0.5, op_b=1)
+        else:
+            ctx.syr2k(prec, n, k, 1.5, dA, k, dB, k, -0.5, dC, n)
+            ref = oracle.gemm_f64(A, B, C, 1.5, -0.5, op_b=1, A2=B, B2=A)
+        ctx.synchronize()
+        assert oracle.error_norms(ctx.download(dC, C.shape), ref)[1] < BOUND[prec], name
+        ctx.free(dC)
+    ctx.config_set(prec, n, n, k, 0)
+    ctx.free(dA)
+    ctx.free(dB)
