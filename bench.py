@@ -33,10 +33,12 @@ import numpy as np  # noqa: E402
 ALPHA, BETA = 32412.0, 2123.0
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
-# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
-# capture of the same kernel and workload (profiles/ holds the summaries).
-# Measured with ncu on the tuned configuration (profiles/split_gemm_bf16x3_n4096_n8192.md).
-TRAFFIC_PER_LAUNCH: dict[tuple[str, int], float] = {("bf16x3_gemm", 4096): 397.3e6, ("bf16x3_gemm", 8192): 2.797e9}
+# DRAM bytes (read + write) per launch of the dominant kernel, keyed by
+# (kernel, N, tile configuration), from one ncu capture of the same kernel,
+# configuration and workload (profiles/split_gemm_bf16x3_n4096_n8192.md).
+TRAFFIC_PER_LAUNCH: dict[tuple[str, int, int], float] = {
+    ("bf16x3_gemm", 4096, 1): 397.3e6, ("bf16x3_gemm", 8192, 1): 2.797e9,
+    ("bf16x3_gemm", 4096, 3): 462.6e6, ("bf16x3_gemm", 8192, 3): 3.163e9}
 
 
 # ------------------------------------------------------------------ helpers
@@ -314,7 +316,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
         bf16 = peaks["bf16_tflops"]
         peak = bf16 / mma_per_mac
         roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
-                "frac": kernel_tflops / peak, "traffic": TRAFFIC_PER_LAUNCH.get((head["dominant_kernel"], n)),
+                "frac": kernel_tflops / peak, "traffic": TRAFFIC_PER_LAUNCH.get((head["dominant_kernel"], n, head["tile_config"])),
                 "kernel": head["dominant_kernel"], "kernel_avg_ms": head["dominant_avg_ms"],
                 "peak_source": f"{bf16} TFLOP/s dense BF16 burst ({peak_kind}) / {mma_per_mac} BF16 MMAs per "
                                f"multiply-add",

@@ -148,6 +148,19 @@ gbpoly_status gbpoly_graph_end(gbpoly_ctx* ctx, gbpoly_graph** graph);
 gbpoly_status gbpoly_graph_launch(gbpoly_ctx* ctx, gbpoly_graph* graph);
 gbpoly_status gbpoly_graph_destroy(gbpoly_ctx* ctx, gbpoly_graph* graph);
 
+/* --------------------------------------------------------- stream hold -- */
+/* Hold the context's stream: work queued after gbpoly_stream_hold starts only
+ * once gbpoly_stream_release is called, or once `timeout_us` microseconds
+ * have passed (a small kernel waits, bounded, on a mapped host word).  The
+ * harness brackets each command group with it so that the command's start
+ * event is timestamped when the command's kernels are already queued: the
+ * event pair then measures device execution, as the reference's
+ * command_start / command_end profiling does (include/common.h:86-99),
+ * instead of including the host's launch latency.  Not for use inside a
+ * graph capture. */
+gbpoly_status gbpoly_stream_hold(gbpoly_ctx* ctx, uint32_t timeout_us);
+gbpoly_status gbpoly_stream_release(gbpoly_ctx* ctx);
+
 /* ----------------------------------------------------------------- events -- */
 
 /* Event handles for kernel-time profiling.  They replace the

@@ -97,6 +97,17 @@ gbpoly_status make_tmap_2d(gbpoly_ctx* ctx, CUtensorMap* map, CUtensorMapDataTyp
   return GBPOLY_OK;
 }
 
+// Holds the stream until the host stores `value` into the mapped word, or
+// until `timeout_ns` have passed (a hold nobody releases ends by itself).
+__global__ void hold_kernel(const volatile unsigned* word, unsigned value, uint64_t timeout_ns) {
+  if(threadIdx.x != 0) return;
+  const uint64_t t0 = global_timer_ns();
+  while(int(*word - value) < 0) {
+    if(global_timer_ns() - t0 > timeout_ns) return;
+    __nanosleep(256);
+  }
+}
+
 }  // namespace gbpoly
 
 using namespace gbpoly;
@@ -164,10 +175,16 @@ gbpoly_status gbpoly_init(int device, gbpoly_ctx** out_ctx) {
     *ctx->err_host = 0;
     e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->err_dev), ctx->err_host, 0);
   }
+  if(e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->hold_host), sizeof(unsigned), cudaHostAllocMapped);
+  if(e == cudaSuccess) {
+    *ctx->hold_host = 0;
+    e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->hold_dev), ctx->hold_host, 0);
+  }
   if(e != cudaSuccess) {
     gbpoly_status st = cuda_fail(e, "context setup");
     if(ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if(ctx->err_host) cudaFreeHost(ctx->err_host);
+    if(ctx->hold_host) cudaFreeHost(ctx->hold_host);
     delete ctx;
     return st;
   }
@@ -198,6 +215,7 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   for(auto e : ctx->event_pool) cudaEventDestroy(e);
   if(ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if(ctx->err_host) cudaFreeHost(ctx->err_host);
+  if(ctx->hold_host) cudaFreeHost(ctx->hold_host);
   delete ctx;
   return GBPOLY_OK;
 }
@@ -422,6 +440,20 @@ gbpoly_status gbpoly_event_elapsed_ms(gbpoly_ctx* ctx, gbpoly_event* start, gbpo
   if(!start || !end || !ms) return fail(GBPOLY_ERR_INVALID, "null argument");
   GBPOLY_CUDA_TRY(cudaEventSynchronize(end->ev));
   GBPOLY_CUDA_TRY(cudaEventElapsedTime(ms, start->ev, end->ev));
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_stream_hold(gbpoly_ctx* ctx, uint32_t timeout_us) {
+  CTX_TRY(ctx);
+  const unsigned value = ++ctx->hold_value;
+  hold_kernel<<<1, 32, 0, ctx->stream>>>(ctx->hold_dev, value, uint64_t(timeout_us) * 1000ull);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_stream_release(gbpoly_ctx* ctx) {
+  CTX_TRY(ctx);
+  __atomic_store_n(ctx->hold_host, ctx->hold_value, __ATOMIC_RELEASE);
   return GBPOLY_OK;
 }
 

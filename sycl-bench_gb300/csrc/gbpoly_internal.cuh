@@ -54,6 +54,11 @@ struct gbpoly_ctx {
   cudaStream_t stream = nullptr;
   int* err_host = nullptr;  // mapped pinned word; kernels write it, host reads after sync
   int* err_dev = nullptr;   // device alias of err_host
+  // stream hold (gbpoly_stream_hold/release): mapped pinned word, its device
+  // alias and the value the next hold waits for
+  unsigned* hold_host = nullptr;
+  unsigned* hold_dev = nullptr;
+  unsigned hold_value = 0;
   int sm_count = 0;
   int sm_clock_khz = 0;
   int cc_major = 0, cc_minor = 0;

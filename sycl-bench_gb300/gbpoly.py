@@ -114,6 +114,8 @@ SIGNATURES: dict[str, tuple] = {
                                    _c_i64]),
     "gbpoly_syr2k_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64,
                                     ct.c_float, _vp, _c_i64]),
+    "gbpoly_stream_hold": (ct.c_int, [_vp, ct.c_uint32]),
+    "gbpoly_stream_release": (ct.c_int, [_vp]),
     "gbpoly_gemv_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, ct.c_float, _vp]),
     "gbpoly_gemv_pair_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_int]),
     "gbpoly_gesummv_f32": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64, _vp, ct.c_float, _vp,
@@ -404,6 +406,13 @@ class Context:
     def syr2k(self, prec, N, K, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
         _check(self.lib.gbpoly_syr2k_f32(self.handle, int(prec), N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta,
                                          _ptr(C), ldc))
+
+    # -- stream hold (device-only timing of a group of launches)
+    def stream_hold(self, timeout_us: int = 20000) -> None:
+        _check(self.lib.gbpoly_stream_hold(self.handle, timeout_us))
+
+    def stream_release(self) -> None:
+        _check(self.lib.gbpoly_stream_release(self.handle))
 
     # -- matrix-vector products (atax, bicg, mvt, gesummv)
     def gemv(self, op, rows, cols, alpha, A, lda, x, beta, y) -> None:

@@ -9,8 +9,9 @@
 // submit() mirrors queue::submit(command group): it hands the command group a
 // Handler that says where to run, and returns an Event carrying the timing
 // data the reference reads through event::get_profiling_info
-// (include/common.h:88-96): device start/end (CUDA events) and the host time
-// the command was submitted.
+// (include/common.h:88-96): device start/end (CUDA events around the
+// command's launches, queued behind a bounded stream hold so that they time
+// device execution) and the host time the command was submitted.
 #pragma once
 
 #include <chrono>
@@ -130,6 +131,9 @@ private:
 class Queue {
 public:
   Queue() = default;
+  // Longest a submitted command group's launches may take to queue before
+  // the stream starts without waiting for them.
+  static constexpr uint32_t kHoldTimeoutUs = 20000;
 
   // "cpu", "gpu" or "default" (include/command_line.h:193-201).  The GPU
   // index is taken from GBPOLY_DEVICE (default 0).
@@ -185,6 +189,14 @@ public:
     check(gbpoly_event_create(impl->ctx, &s), "event create");
     check(gbpoly_event_create(impl->ctx, &e), "event create");
     Event ev(impl, s, e, submit);
+    // The stream waits (bounded) until the command group is queued, so the
+    // start event is timestamped when its kernels can start: the pair times
+    // device execution, not the host's launch latency.
+    check(gbpoly_stream_hold(impl->ctx, kHoldTimeoutUs), "stream hold");
+    struct Release {
+      gbpoly_ctx* ctx;
+      ~Release() { gbpoly_stream_release(ctx); }
+    } release{impl->ctx};
     check(gbpoly_event_record(impl->ctx, s), "event record");
     cg(h);
     check(gbpoly_event_record(impl->ctx, e), "event record");
