@@ -633,11 +633,11 @@ def run_neighbours(ctx, args) -> dict:
         dB = ctx.upload(A[::-1].copy()) if name == "gesummv" else None
         a64 = A.astype(np.float64)
         if name == "atax":
+            # tmp += A x, y += A^T tmp in one call; from zero tmp and y the first call gives A^T A x
             def step():
-                ctx.gemv(Op.N, m, m, 1.0, dA, m, d1, 0.0, y1)
-                ctx.gemv(Op.T, m, m, 1.0, dA, m, y1, 0.0, y2)
+                ctx.atax(m, m, dA, m, d1, y1, y2)
             t = a64 @ v1.astype(np.float64)
-            refs, outs, passes = [a64.T @ t], [y2], 2
+            refs, outs, passes = [a64.T @ t], [y2], 1
         elif name == "bicg":
             def step():
                 ctx.gemv_pair(m, m, dA, m, [(Op.T, 1.0, 0.0, d1, y1), (Op.N, 1.0, 0.0, d2, y2)])

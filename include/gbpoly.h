@@ -237,6 +237,15 @@ gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N
 gbpoly_status gbpoly_gemv_f32(gbpoly_ctx* ctx, gbpoly_op op, int64_t rows, int64_t cols, float alpha, const float* A,
     int64_t lda, const float* x, float beta, float* y);
 
+/* tmp <- tmp + A x, then y <- y + A^T tmp (the updated tmp).  Replaces
+ * Atax1 + Atax2 (polybench/atax.cpp:73-97).  Up to 8192 columns (16-byte
+ * aligned rows and x) one kernel reads each row of A from HBM once: a CTA
+ * completes a row group's dots, then reads the same rows again (from L2)
+ * for the column sums; wider or unaligned matrices take two
+ * gbpoly_gemv_f32 passes. */
+gbpoly_status gbpoly_atax_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* A, int64_t lda, const float* x,
+    float* tmp, float* y);
+
 /* One product y <- beta * y + alpha * op(A) x of a pair. */
 typedef struct {
   gbpoly_op op;

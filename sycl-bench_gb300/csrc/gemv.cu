@@ -267,6 +267,110 @@ gbpoly_status launch_gemv(gbpoly_ctx* ctx, GemvArgs g, Term r0, Term r1, Term ct
   return GBPOLY_OK;
 }
 
+// atax in one kernel: tmp += A x, then y += A^T tmp, each row group's rows
+// read from HBM once.  A persistent CTA walks row groups of kAtaxRows rows:
+// phase 1 reads the group's rows over all column chunks and completes their
+// row dots (so tmp of those rows is final), phase 2 reads the same rows again
+// (just read: from L2) and adds A[r][c] tmp[r] into the thread's column
+// accumulators, which stay in registers across the CTA's row groups and are
+// written once as the CTA's partial row of col_part.  CHUNKS 1024-column
+// chunks (cols <= CHUNKS * 1024, at most 8), 128-bit loads, one CTA per SM.
+constexpr int kAtaxRows = 16;
+
+template <int CHUNKS>
+__global__ void __launch_bounds__(kThreads, 1) atax_kernel(const float* __restrict__ A, int64_t lda, int rows, int cols,
+    const float* __restrict__ x, float* __restrict__ tmp, float* __restrict__ col_part, int groups) {
+  __shared__ float red[kThreads / 32][kAtaxRows];
+  __shared__ float tmp_s[kAtaxRows];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float4 xr[CHUNKS], colacc[CHUNKS];
+#pragma unroll
+  for(int ch = 0; ch < CHUNKS; ++ch) {
+    const int c = ch * kTileCols + 4 * tid;
+    xr[ch] = c < cols ? *reinterpret_cast<const float4*>(x + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+    colacc[ch] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for(int g = blockIdx.x; g < groups; g += gridDim.x) {
+    const int r0 = g * kAtaxRows, nr = min(kAtaxRows, rows - r0);
+    // phase 1: row dots of the group over all columns
+    float acc[kAtaxRows];
+#pragma unroll
+    for(int k = 0; k < kAtaxRows; ++k) acc[k] = 0.f;
+#pragma unroll
+    for(int ch = 0; ch < CHUNKS; ++ch) {
+      const int c = ch * kTileCols + 4 * tid;
+      if(c < cols) {
+        float4 a[kAtaxRows];
+#pragma unroll
+        for(int k = 0; k < kAtaxRows; ++k)
+          a[k] = k < nr ? *reinterpret_cast<const float4*>(A + int64_t(r0 + k) * lda + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for(int k = 0; k < kAtaxRows; ++k) acc[k] += dot4(a[k], xr[ch]);
+      }
+    }
+    const float rs = reduce_rows<kAtaxRows>(acc, lane);
+    if(lane < kAtaxRows) red[warp][lane] = rs;
+    __syncthreads();
+    if(warp == 0 && lane < kAtaxRows) {
+      float sum = 0.f;
+#pragma unroll
+      for(int w = 0; w < kThreads / 32; ++w) sum += red[w][lane];
+      float t = 0.f;
+      if(lane < nr) {
+        t = tmp[r0 + lane] + sum;  // tmp += A x (atax.cpp:78-83)
+        tmp[r0 + lane] = t;
+      }
+      tmp_s[lane] = t;
+    }
+    __syncthreads();
+    // phase 2: the same rows again, y += A^T tmp (atax.cpp:91-96)
+#pragma unroll
+    for(int ch = 0; ch < CHUNKS; ++ch) {
+      const int c = ch * kTileCols + 4 * tid;
+      if(c < cols) {
+        float4 a[kAtaxRows];
+#pragma unroll
+        for(int k = 0; k < kAtaxRows; ++k)
+          a[k] = k < nr ? *reinterpret_cast<const float4*>(A + int64_t(r0 + k) * lda + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for(int k = 0; k < kAtaxRows; ++k) {
+          const float w = tmp_s[k];
+          colacc[ch].x = fmaf(a[k].x, w, colacc[ch].x);
+          colacc[ch].y = fmaf(a[k].y, w, colacc[ch].y);
+          colacc[ch].z = fmaf(a[k].z, w, colacc[ch].z);
+          colacc[ch].w = fmaf(a[k].w, w, colacc[ch].w);
+        }
+      }
+    }
+    __syncthreads();  // red and tmp_s are rewritten by the next group
+  }
+#pragma unroll
+  for(int ch = 0; ch < CHUNKS; ++ch) {
+    const int c = ch * kTileCols + 4 * tid;
+    if(c < cols) *reinterpret_cast<float4*>(col_part + int64_t(blockIdx.x) * cols + c) = colacc[ch];
+  }
+}
+
+template <int CHUNKS>
+gbpoly_status launch_atax(gbpoly_ctx* ctx, const float* A, int64_t lda, int rows, int cols, const float* x, float* tmp,
+    float* y) {
+  const int groups = (rows + kAtaxRows - 1) / kAtaxRows;
+  const int grid = std::max(1, std::min(groups, std::max(ctx->sm_count, 1)));  // one CTA per SM
+  gbpoly_status st = ensure_scratch(ctx, ctx->stats, size_t(grid) * size_t(cols) * 4 + 256, "matrix-vector scratch");
+  if(st != GBPOLY_OK) return st;
+  float* col_part = static_cast<float*>(ctx->stats.ptr);
+  {
+    ProfileScope prof(ctx, "atax");
+    atax_kernel<CHUNKS><<<grid, kThreads, 0, ctx->stream>>>(A, lda, rows, cols, x, tmp, col_part, groups);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+  }
+  ProfileScope prof(ctx, "gemv_final");
+  gemv_final_kernel<0, true, false><<<unsigned((cols + 31) / 32), 256, 0, ctx->stream>>>(nullptr, 0, rows, col_part,
+      grid, cols, Term{}, Term{}, Term{1.f, 1.f, y});
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
 gbpoly_status check_common(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* A, int64_t lda) {
   if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
   GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
@@ -322,6 +426,32 @@ gbpoly_status gbpoly_gemv_f32(gbpoly_ctx* ctx, gbpoly_op op, int64_t rows, int64
     int64_t lda, const float* x, float beta, float* y) {
   gbpoly_gemv_term t{op, alpha, beta, x, y};
   return gbpoly_gemv_pair_f32(ctx, rows, cols, A, lda, &t, 1);
+}
+
+gbpoly_status gbpoly_atax_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, const float* A, int64_t lda, const float* x,
+    float* tmp, float* y) {
+  gbpoly_status st = check_common(ctx, rows, cols, A, lda);
+  if(st != GBPOLY_OK) return st;
+  if((cols > 0 && (!x || !y)) || (rows > 0 && !tmp)) return fail(GBPOLY_ERR_INVALID, "vector: null pointer");
+  if(rows == 0 || cols == 0) return GBPOLY_OK;  // empty sums: tmp and y unchanged
+  const bool vec = (cols % 4 == 0) && (lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+  const int chunks = int((cols + kTileCols - 1) / kTileCols);
+  if(vec && chunks <= 8) {
+    switch(chunks) {
+    case 1: return launch_atax<1>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 2: return launch_atax<2>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 3: return launch_atax<3>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 4: return launch_atax<4>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 5: return launch_atax<5>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 6: return launch_atax<6>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    case 7: return launch_atax<7>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    default: return launch_atax<8>(ctx, A, lda, int(rows), int(cols), x, tmp, y);
+    }
+  }
+  // wide or unaligned matrices: the two passes
+  if((st = gbpoly_gemv_f32(ctx, GBPOLY_OP_N, rows, cols, 1.f, A, lda, x, 1.f, tmp)) != GBPOLY_OK) return st;
+  return gbpoly_gemv_f32(ctx, GBPOLY_OP_T, rows, cols, 1.f, A, lda, tmp, 1.f, y);
 }
 
 gbpoly_status gbpoly_gesummv_f32(gbpoly_ctx* ctx, int64_t rows, int64_t cols, float alpha, const float* A,

@@ -117,6 +117,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_stream_hold": (ct.c_int, [_vp, ct.c_uint32]),
     "gbpoly_stream_release": (ct.c_int, [_vp]),
     "gbpoly_gemv_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, ct.c_float, _vp]),
+    "gbpoly_atax_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, _vp]),
     "gbpoly_gemv_pair_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_int]),
     "gbpoly_gesummv_f32": (ct.c_int, [_vp, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, _c_i64, _vp, ct.c_float, _vp,
                                       _vp]),
@@ -417,6 +418,9 @@ class Context:
     # -- matrix-vector products (atax, bicg, mvt, gesummv)
     def gemv(self, op, rows, cols, alpha, A, lda, x, beta, y) -> None:
         _check(self.lib.gbpoly_gemv_f32(self.handle, int(op), rows, cols, alpha, _ptr(A), lda, _ptr(x), beta, _ptr(y)))
+
+    def atax(self, rows, cols, A, lda, x, tmp, y) -> None:
+        _check(self.lib.gbpoly_atax_f32(self.handle, rows, cols, _ptr(A), lda, _ptr(x), _ptr(tmp), _ptr(y)))
 
     def gemv_pair(self, rows, cols, A, lda, terms) -> None:
         """terms: up to two (op, alpha, beta, x, y) tuples, all over one pass of A."""

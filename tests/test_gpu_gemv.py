@@ -44,6 +44,38 @@ def test_atax_verifies(ctx, n):
         ctx.free(b)
 
 
+@pytest.mark.parametrize("n", SIZES + [4096, 4100, 5000, 8192, 8196])
+def test_atax_one_call_verifies(ctx, n):
+    # gbpoly_atax_f32: one kernel up to 8192 aligned columns, two passes beyond or unaligned
+    A, x = oracle.init_atax(n)
+    dA, dx = ctx.upload(A), ctx.upload(x)
+    dt, dy = ctx.upload(np.zeros(n, np.float32)), ctx.upload(np.zeros(n, np.float32))
+    ctx.atax(n, n, dA, n, dx, dt, dy)
+    ctx.synchronize()
+    assert_verifies(oracle.host_atax(n), ctx.download(dy, (n,)))
+    for b in (dA, dx, dt, dy):
+        ctx.free(b)
+
+
+@pytest.mark.parametrize("rows,cols", [(3001, 4096), (17, 1024), (4096, 3072), (1000, 2052)])
+def test_atax_seeded_against_fp64(ctx, rows, cols):
+    rng = np.random.default_rng(rows + cols)
+    A = rng.standard_normal((rows, cols)).astype(np.float32)
+    x = rng.standard_normal(cols).astype(np.float32)
+    t0 = rng.standard_normal(rows).astype(np.float32)
+    y0 = rng.standard_normal(cols).astype(np.float32)
+    dA, dx, dt, dy = ctx.upload(A), ctx.upload(x), ctx.upload(t0), ctx.upload(y0)
+    ctx.atax(rows, cols, dA, cols, dx, dt, dy)
+    ctx.synchronize()
+    a = A.astype(np.float64)
+    t = t0 + a @ x.astype(np.float64)
+    y = y0 + a.T @ t
+    assert rel(ctx.download(dt, (rows,)), t) < 1e-5
+    assert rel(ctx.download(dy, (cols,)), y) < 1e-5
+    for b in (dA, dx, dt, dy):
+        ctx.free(b)
+
+
 @pytest.mark.parametrize("n", SIZES)
 def test_bicg_verifies(ctx, n):
     A, p, r = oracle.init_bicg(n)
