@@ -107,7 +107,9 @@ gbpoly_status gbpoly_memset(gbpoly_ctx* ctx, void* dst, int value, size_t bytes)
  * least `bytes` large now, so that later calls of that size do not allocate.
  * Needed before capturing tensor-core calls into a graph.  Synchronises. */
 gbpoly_status gbpoly_workspace_reserve(gbpoly_ctx* ctx, size_t bytes);
-/* Workspace bytes a contraction of this shape and form needs (0 for fp32). */
+/* Workspace bytes a contraction of this shape and form needs (fp32: the
+ * partial products of its K split, used when the output tiles are too few
+ * to fill the device; 0 otherwise). */
 gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, int same_operand,
     size_t* bytes);
 

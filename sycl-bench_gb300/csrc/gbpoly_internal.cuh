@@ -131,6 +131,10 @@ struct GemmF32Args {
   int64_t lda2 = 0;
   const float* B2 = nullptr;
   int64_t ldb2 = 0;
+  // FP32 only: K split count (0: chosen from the shape; 1: none).  Callers
+  // that run a contraction in row panels pass the full shape's split so the
+  // panels add K in the same order as the whole call.
+  int ksplit = 0;
 };
 // op(B) is op(A)^T on the same stored matrix (syrk's A.A^T, covariance's
 // X^T.X): the product is symmetric, and one set of split panels serves both
@@ -139,6 +143,12 @@ inline bool symmetric_operand(const GemmF32Args& a) {
   return !a.dual && a.A == a.B && a.lda == a.ldb && a.M == a.N && a.op_a != a.op_b;
 }
 gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a);
+// Workspace of the K split the FP32 kernel uses for grids too small to fill a
+// device of `sm_count` SMs (0 when it does not split).
+size_t fp32_split_k_bytes(int sm_count, int64_t M, int64_t N, int64_t K);
+// The K split count gbpoly_gemm_f32 uses for an FP32 contraction of this
+// shape on operands the TMA kernel can read (1: no split).
+int fp32_split_k_count(int sm_count, int64_t M, int64_t N, int64_t K);
 // Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
 // term panels live in the context workspace.
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a);

@@ -121,8 +121,15 @@ extern "C" gbpoly_status gbpoly_gemm_f32_host(gbpoly_ctx* ctx, gbpoly_precision 
     GemmF32Args a{};
     a.M = pipelined ? rows : M, a.N = N, a.K = K, a.alpha = alpha, a.beta = beta, a.op_a = op_a, a.op_b = op_b;
     a.A = pipelined ? dA + r0 * K : dA, a.lda = ac, a.B = dB, a.ldb = bc, a.C = dC + r0 * N, a.ldc = N;
-    if(prec == GBPOLY_PREC_FP32)
+    if(prec == GBPOLY_PREC_FP32) {
+      // the K split of the whole call on equally aligned device operands
+      // (operands the TMA kernel cannot read are not split), so the panels
+      // give the device-buffer call's bits
+      const bool tma_like = ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) == 0 &&
+                            lda % 4 == 0 && ldb % 4 == 0;
+      a.ksplit = tma_like ? fp32_split_k_count(ctx->sm_count, M, N, K) : 1;
       st = launch_gemm_f32_simt(ctx, a);
+    }
     else
       st = tensor_plan_panel(ctx, plan, a, p == 0, r0);
     if(st != GBPOLY_OK) return st;

@@ -124,7 +124,7 @@ __device__ __forceinline__ void lower_coords(int t, int& tile_m, int& tile_n) {
 template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
 __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_constant__ CUtensorMap tmA,
     const __grid_constant__ CUtensorMap tmB, int M, int N, int K, float alpha, float beta, float* __restrict__ C,
-    int64_t ldc, int lower, int* err) {
+    int64_t ldc, int lower, int kt_per_split, float* __restrict__ part, int* err) {
   constexpr int kTilesPerStage = DUAL ? 4 : 2;
   constexpr int kStageBytes = kTilesPerStage * kTileBytes;
   extern __shared__ __align__(1024) char smem_raw[];
@@ -143,7 +143,17 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
     tile_coords(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
   const int m0 = tile_m * kBM, n0 = tile_n * kBN;
   const bool mirror = lower && tile_m != tile_n;
+  // split K (gridDim.y > 1): this CTA covers k tiles [kt0, kt0 + nkt) and
+  // writes alpha * its partial product to its slice of `part` (M x N, ld N);
+  // a reduction kernel adds the slices and beta * C
   const int ktiles = (K + kBK - 1) / kBK;
+  const int kt0 = int(blockIdx.y) * kt_per_split;
+  const int nkt = max(0, min(ktiles, kt0 + kt_per_split) - kt0);
+  if(gridDim.y > 1) {
+    C = part + int64_t(blockIdx.y) * int64_t(M) * N;
+    ldc = N;
+    beta = 0.f;
+  }
 
   if(tid == 0) {
 #pragma unroll
@@ -161,12 +171,12 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
       int issued = 0;
-      for(int kt = 0; kt < ktiles; ++kt) {
-        const int s = kt % STAGES;
-        if(kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, err, kDevErrEmptyWait)) break;
+      for(int i = 0; i < nkt; ++i) {
+        const int s = i % STAGES;
+        if(i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1, err, kDevErrEmptyWait)) break;
         char* st = smem + s * kStageBytes;
         mbar_arrive_expect_tx(&full[s], kStageBytes);
-        const int k0 = kt * kBK;
+        const int k0 = (kt0 + i) * kBK;
         if constexpr(DUAL) {
           tma_load_2d(st + 0 * kTileBytes, &tmA, &full[s], k0, m0);  // A rows of the C tile
           tma_load_2d(st + 1 * kTileBytes, &tmB, &full[s], k0, n0);  // B rows of the C tile columns
@@ -202,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
     for(int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
   bool ok = true;
-  for(int kt = 0; kt < ktiles; ++kt) {
+  for(int kt = 0; kt < nkt; ++kt) {
     const int s = kt % STAGES;
     if(!mbar_wait(&full[s], (kt / STAGES) & 1, err, kDevErrFullWait)) {
       ok = false;
@@ -295,6 +305,31 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
   }
 }
 
+// C = sum over the splits of part[s] (already scaled by alpha) + beta C, the
+// splits added in index order.
+__global__ void split_k_reduce_kernel(const float* __restrict__ part, int splits, int M, int N, float beta, float* C,
+    int64_t ldc) {
+  const int64_t total = int64_t(M) * N;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for(int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += stride) {
+    const int64_t m = e / N, n = e - m * N;
+    float s = 0.f;
+    for(int k = 0; k < splits; ++k) s += part[int64_t(k) * total + e];
+    float* c = C + m * ldc + n;
+    *c = beta != 0.f ? fmaf(beta, *c, s) : s;
+  }
+}
+
+// K split for grids too small to fill the device: about one CTA per SM, at
+// least 4 k tiles (128 of K) per split, at most 8 splits.
+int split_k_count(int sm_count, int64_t tiles, int64_t ktiles) {
+  if(tiles <= 0 || tiles * 2 > sm_count || ktiles < 8) return 1;
+  int64_t s = std::min<int64_t>(std::min<int64_t>(sm_count / tiles, ktiles / 4), 8);
+  if(s <= 1) return 1;
+  const int64_t per = (ktiles + s - 1) / s;
+  return int((ktiles + per - 1) / per);  // every split non-empty
+}
+
 template <bool A_KMAJ, bool B_KMAJ, bool DUAL, int STAGES>
 gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMap& ta, const CUtensorMap& tb,
     bool lower) {
@@ -311,12 +346,52 @@ gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMa
     const int64_t t = (a.M + kBM - 1) / kBM;
     tiles = t * (t + 1) / 2;
   }
-  ProfileScope prof(ctx, DUAL ? "sgemm_simt_dual" : "sgemm_simt");
-  kern<<<static_cast<unsigned>(tiles), kThreads, kSmem, ctx->stream>>>(ta, tb, static_cast<int>(a.M),
-      static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc, lower ? 1 : 0, ctx->err_dev);
-  GBPOLY_CUDA_TRY(cudaGetLastError());
+  // the split depends on the full square's tile count, so a symmetric product
+  // splits K exactly like the same product computed in full (same bits)
+  const int64_t ktiles = (a.K + kBK - 1) / kBK;
+  int splits = a.ksplit > 0 ? int(std::min<int64_t>(a.ksplit, std::max<int64_t>(ktiles, 1)))
+                            : split_k_count(ctx->sm_count, ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN), ktiles);
+  const int kt_per_split = int((ktiles + splits - 1) / splits);
+  splits = int((ktiles + kt_per_split - 1) / kt_per_split);  // every split non-empty
+  if(splits < 1) splits = 1;
+  float* part = nullptr;
+  if(splits > 1) {
+    gbpoly_status st = ensure_workspace(ctx, size_t(splits) * size_t(a.M) * size_t(a.N) * sizeof(float));
+    if(st != GBPOLY_OK) return st;
+    part = static_cast<float*>(ctx->ws.ptr);
+  }
+  {
+    ProfileScope prof(ctx, DUAL ? "sgemm_simt_dual" : "sgemm_simt");
+    kern<<<dim3(static_cast<unsigned>(tiles), static_cast<unsigned>(splits)), kThreads, kSmem, ctx->stream>>>(ta, tb,
+        static_cast<int>(a.M), static_cast<int>(a.N), static_cast<int>(a.K), a.alpha, a.beta, a.C, a.ldc,
+        lower ? 1 : 0, kt_per_split, part, ctx->err_dev);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+  }
+  if(splits > 1) {
+    ProfileScope prof(ctx, "split_k_reduce");
+    const int64_t total = a.M * a.N;
+    const unsigned blocks = unsigned(std::min<int64_t>((total + 255) / 256, 8ll * ctx->sm_count));
+    split_k_reduce_kernel<<<blocks, 256, 0, ctx->stream>>>(part, splits, int(a.M), int(a.N), a.beta, a.C, a.ldc);
+    GBPOLY_CUDA_TRY(cudaGetLastError());
+  }
   return GBPOLY_OK;
 }
+
+}  // namespace
+
+// Workspace bytes of the K split of an FP32 contraction, for a device of at
+// most `sm_count` SMs (more SMs never need less).
+int fp32_split_k_count(int sm_count, int64_t M, int64_t N, int64_t K) {
+  return split_k_count(sm_count, ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN), (K + kBK - 1) / kBK);
+}
+
+size_t fp32_split_k_bytes(int sm_count, int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + kBM - 1) / kBM) * ((N + kBN - 1) / kBN);
+  const int s = split_k_count(sm_count, tiles, (K + kBK - 1) / kBK);
+  return s > 1 ? size_t(s) * size_t(M) * size_t(N) * sizeof(float) : 0;
+}
+
+namespace {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 

@@ -917,6 +917,9 @@ size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, b
     return align_up(size_t(M) * Kp, 1024) + (same ? 0 : align_up(size_t(N) * Kp, 1024)) +
            align_up(size_t((M + 127) / 128) * kb * 4, 256) + (same ? 0 : align_up(size_t((N + 127) / 128) * kb * 4, 256));
   }
+  case GBPOLY_PREC_FP32:
+    // partial products of the K split of small grids, bounded for devices of up to 256 SMs
+    return fp32_split_k_bytes(256, M, N, K);
   default: return 0;
   }
 }
@@ -1204,9 +1207,17 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
   g->descs.assign(descs, descs + count);
   gbpoly_status st = GBPOLY_OK;
   switch(prec) {
-  case GBPOLY_PREC_FP32:
-    for(auto& d : g->descs) g->flops += 2 * d.M * d.N * d.K;
+  case GBPOLY_PREC_FP32: {
+    // per-problem launches; the workspace their K splits need is reserved now
+    // so that running the plan (or capturing it) allocates nothing
+    size_t ws = 0;
+    for(auto& d : g->descs) {
+      g->flops += 2 * d.M * d.N * d.K;
+      ws = std::max(ws, fp32_split_k_bytes(ctx->sm_count, d.M, d.N, d.K));
+    }
+    if(ws > 0) st = ensure_workspace(ctx, ws);
     break;
+  }
   case GBPOLY_PREC_BF16X3: st = plan_grouped<GroupBF16x3>(ctx, g); break;
   case GBPOLY_PREC_TF32X3: st = plan_grouped<GroupTF32x3>(ctx, g); break;
   case GBPOLY_PREC_BF16X6: st = plan_grouped<GroupBF16x6>(ctx, g); break;
