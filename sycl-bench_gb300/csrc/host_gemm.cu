@@ -73,11 +73,13 @@ extern "C" gbpoly_status gbpoly_gemm_f32_host(gbpoly_ctx* ctx, gbpoly_precision 
   float* dB = static_cast<float*>(ctx->stage_b);
   float* dC = static_cast<float*>(ctx->stage_c);
 
-  // Row panels of C (and of op(A) when A is stored row by row): about three
-  // rounds of tiles per panel, at most eight panels.
+  // Row panels of C (and of op(A) when A is stored row by row), at most 16 of
+  // at least 512 rows (a multiple of the 256-row tiles of CTA pairs): the
+  // copies are the bound, and what stays exposed after the last input copy
+  // is one panel's contraction and read-back.
   const bool pipelined = op_a == GBPOLY_OP_N;
-  int panels = pipelined ? int(std::min<int64_t>(8, std::max<int64_t>(1, M / 2048))) : 1;
-  const int64_t rows_per = ((M + panels - 1) / panels + 127) / 128 * 128;
+  int panels = pipelined ? int(std::min<int64_t>(16, std::max<int64_t>(1, M / 512))) : 1;
+  const int64_t rows_per = ((M + panels - 1) / panels + 255) / 256 * 256;
   panels = int((M + rows_per - 1) / rows_per);
 
   cudaEvent_t ev_in = nullptr, ev_done = nullptr;
