@@ -172,34 +172,45 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ X, int64_t 
   // contiguous dimension; 128-bit loads when the block is whole and aligned.
   const int64_t r_lim = R - r0, k_lim = K - k0;
   const bool whole = r_lim >= 64 && k_lim >= 64 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  // (all of a thread's loads are issued before its shared-memory stores)
   if(whole) {
+    float4 v[4];
 #pragma unroll
     for(int e = 0; e < 4; ++e) {
-      const int idx = tid + e * 256;          // 0..1023 float4 of the block
+      const int idx = tid + e * 256;  // 0..1023 float4 of the block
       const int outer = idx >> 4, inner = (idx & 15) * 4;
-      if(k_major) {  // rows of X are rows of op(X): read along k
-        const float4 v = *reinterpret_cast<const float4*>(X + (r0 + outer) * ld + k0 + inner);
-        tile[outer][inner] = v.x;
-        tile[outer][inner + 1] = v.y;
-        tile[outer][inner + 2] = v.z;
-        tile[outer][inner + 3] = v.w;
-      } else {  // rows of X are k: read along r
-        const float4 v = *reinterpret_cast<const float4*>(X + (k0 + outer) * ld + r0 + inner);
-        tile[inner][outer] = v.x;
-        tile[inner + 1][outer] = v.y;
-        tile[inner + 2][outer] = v.z;
-        tile[inner + 3][outer] = v.w;
+      v[e] = k_major ? *reinterpret_cast<const float4*>(X + (r0 + outer) * ld + k0 + inner)   // read along k
+                     : *reinterpret_cast<const float4*>(X + (k0 + outer) * ld + r0 + inner);  // read along r
+    }
+#pragma unroll
+    for(int e = 0; e < 4; ++e) {
+      const int idx = tid + e * 256;
+      const int outer = idx >> 4, inner = (idx & 15) * 4;
+      if(k_major) {
+        tile[outer][inner] = v[e].x;
+        tile[outer][inner + 1] = v[e].y;
+        tile[outer][inner + 2] = v[e].z;
+        tile[outer][inner + 3] = v[e].w;
+      } else {
+        tile[inner][outer] = v[e].x;
+        tile[inner + 1][outer] = v[e].y;
+        tile[inner + 2][outer] = v[e].z;
+        tile[inner + 3][outer] = v[e].w;
       }
     }
   } else {
+    float v[16];
 #pragma unroll
     for(int e = 0; e < 16; ++e) {
       const int idx = tid + e * 256;
       const int rr = k_major ? (idx >> 6) : (idx & 63);
       const int kk = k_major ? (idx & 63) : (idx >> 6);
-      float v = 0.f;
-      if(rr < r_lim && kk < k_lim) v = k_major ? X[(r0 + rr) * ld + k0 + kk] : X[(k0 + kk) * ld + r0 + rr];
-      tile[rr][kk] = v;
+      v[e] = (rr < r_lim && kk < k_lim) ? (k_major ? X[(r0 + rr) * ld + k0 + kk] : X[(k0 + kk) * ld + r0 + rr]) : 0.f;
+    }
+#pragma unroll
+    for(int e = 0; e < 16; ++e) {
+      const int idx = tid + e * 256;
+      tile[k_major ? (idx >> 6) : (idx & 63)][k_major ? (idx & 63) : (idx >> 6)] = v[e];
     }
   }
   __syncthreads();
@@ -244,19 +255,14 @@ struct SplitJob {
   int block_start, kblocks;
 };
 
+// block_job[b]: the job block b belongs to (a table written by the plan, so
+// a block starts its copy after two dependent loads rather than a search)
 template <Elem E, int TERMS>
-__global__ void __launch_bounds__(256) grouped_split_kernel(const SplitJob* __restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(256) grouped_split_kernel(const SplitJob* __restrict__ jobs,
+    const int* __restrict__ block_job) {
   __shared__ float tile[64][65];
   const int b = blockIdx.x;
-  int lo = 0, hi = njobs - 1;  // last job with block_start <= b
-  while(lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if(jobs[mid].block_start <= b)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  const SplitJob j = jobs[lo];
+  const SplitJob j = jobs[block_job[b]];
   const int local = b - j.block_start;
   split_tile<E, TERMS>(j.X, j.ld, j.k_major, j.R, j.K, j.Kp, static_cast<typename Term<E>::T*>(j.out),
       j.panel_stride, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, tile);
@@ -1083,6 +1089,7 @@ struct gbpoly_grouped {
   gbpoly::ProductMaps* maps = nullptr;
   int4* tiles = nullptr;
   gbpoly::SplitJob* jobs = nullptr;
+  int* block_job = nullptr;  // split block -> job
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
 };
@@ -1116,7 +1123,14 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   std::stable_sort(tiles.begin(), tiles.end(), [&](const int4& u, const int4& v) { return kp[u.x] > kp[v.x]; });
   const size_t tiles_off = align_up(maps_off + P * sizeof(ProductMaps), 256);
   const size_t jobs_off = align_up(tiles_off + tiles.size() * sizeof(int4), 256);
-  const size_t total = jobs_off + 2 * P * sizeof(SplitJob);
+  int64_t nblocks = 0;  // split blocks of all operands
+  for(int i = 0; i < P; ++i) {
+    const auto& d = g->descs[i];
+    if(d.M > 0 && d.N > 0) nblocks += ((d.M + 63) / 64 + (d.N + 63) / 64) * (kp[i] / 64);
+  }
+  if(nblocks >= (1ll << 31)) return fail(GBPOLY_ERR_UNSUPPORTED, "too many split blocks in one grouped plan");
+  const size_t table_off = align_up(jobs_off + 2 * P * sizeof(SplitJob), 256);
+  const size_t total = table_off + size_t(nblocks) * sizeof(int);
   GBPOLY_CUDA_TRY(cudaMalloc(&g->dev, total));
   g->dev_bytes = total;
   char* base = static_cast<char*>(g->dev);
@@ -1147,9 +1161,18 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   g->maps = reinterpret_cast<ProductMaps*>(base + maps_off);
   g->tiles = reinterpret_cast<int4*>(base + tiles_off);
   g->jobs = reinterpret_cast<SplitJob*>(base + jobs_off);
+  g->block_job = reinterpret_cast<int*>(base + table_off);
   g->ntiles = int(tiles.size());
   g->njobs = int(jobs.size());
   g->split_blocks = blocks;
+  std::vector<int> owner(size_t(blocks), 0);
+  for(size_t jb = 0; jb < jobs.size(); ++jb) {
+    const int first_block = jobs[jb].block_start;
+    const int end_block = jb + 1 < jobs.size() ? jobs[jb + 1].block_start : blocks;
+    std::fill(owner.begin() + first_block, owner.begin() + end_block, int(jb));
+  }
+  if(!owner.empty())
+    GBPOLY_CUDA_TRY(cudaMemcpy(g->block_job, owner.data(), owner.size() * sizeof(int), cudaMemcpyHostToDevice));
   GBPOLY_CUDA_TRY(cudaMemcpy(g->probs, probs.data(), P * sizeof(GroupProblem), cudaMemcpyHostToDevice));
   GBPOLY_CUDA_TRY(cudaMemcpy(g->maps, maps.data(), P * sizeof(ProductMaps), cudaMemcpyHostToDevice));
   if(!tiles.empty())
@@ -1164,7 +1187,7 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
   using T = typename Term<F::elem>::T;
   if(g->split_blocks > 0) {
     ProfileScope prof(ctx, "grouped_split");
-    grouped_split_kernel<F::elem, F::terms><<<g->split_blocks, 256, 0, ctx->stream>>>(g->jobs, g->njobs);
+    grouped_split_kernel<F::elem, F::terms><<<g->split_blocks, 256, 0, ctx->stream>>>(g->jobs, g->block_job);
     GBPOLY_CUDA_TRY(cudaGetLastError());
   }
   (void)sizeof(T);
