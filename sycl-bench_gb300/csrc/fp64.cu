@@ -114,7 +114,10 @@ gbpoly_status gbpoly_gemm_f64(gbpoly_ctx* ctx, gbpoly_op op_a, gbpoly_op op_b, i
   if((st = check_mat("C", C, M, N, ldc)) != GBPOLY_OK) return st;
   // op(B)[k][n] is addressed as TiledOperand over (n, k)
   TiledOperand<double> ob = op_b == GBPOLY_OP_N ? TiledOperand<double>{B, 1, ldb} : TiledOperand<double>{B, ldb, 1};
-  return launch_tiled_gemm<double>(ctx, M, N, K, alpha, opnd(A, lda, op_a), ob, false, {}, {}, beta, C, ldc);
+  // op(B) = op(A)^T on the same matrix (syrk's A.A^T, X^T.X): symmetric, lower triangle of tiles + mirror
+  const bool symmetric = A == B && lda == ldb && M == N && op_a != op_b;
+  return launch_tiled_gemm<double>(ctx, M, N, K, alpha, opnd(A, lda, op_a), ob, false, {}, {}, beta, C, ldc,
+      symmetric);
 }
 
 gbpoly_status gbpoly_syrk_f64(gbpoly_ctx* ctx, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
@@ -133,7 +136,7 @@ gbpoly_status gbpoly_syr2k_f64(gbpoly_ctx* ctx, int64_t N, int64_t K, double alp
   if((st = check_mat("C", C, N, N, ldc)) != GBPOLY_OK) return st;
   return launch_tiled_gemm<double>(ctx, N, N, K, alpha, TiledOperand<double>{A, lda, 1},
       TiledOperand<double>{B, ldb, 1}, true, TiledOperand<double>{B, ldb, 1}, TiledOperand<double>{A, lda, 1}, beta,
-      C, ldc);
+      C, ldc, true);  // symmetric: lower triangle of tiles + mirror
 }
 
 gbpoly_status gbpoly_convert_f32_f64(gbpoly_ctx* ctx, const float* src, double* dst, int64_t count) {

@@ -409,7 +409,8 @@ gbpoly_status launch_gemm_f32_simt(gbpoly_ctx* ctx, const GemmF32Args& a) {
     TiledOperand<float> oa = a_kmaj ? TiledOperand<float>{a.A, a.lda, 1} : TiledOperand<float>{a.A, 1, a.lda};
     TiledOperand<float> ob = b_kmaj ? TiledOperand<float>{a.B, a.ldb, 1} : TiledOperand<float>{a.B, 1, a.ldb};
     TiledOperand<float> oa2{a.A2, a.lda2, 1}, ob2{a.B2, a.ldb2, 1};
-    return launch_tiled_gemm<float>(ctx, a.M, a.N, a.K, a.alpha, oa, ob, a.dual, oa2, ob2, a.beta, a.C, a.ldc);
+    return launch_tiled_gemm<float>(ctx, a.M, a.N, a.K, a.alpha, oa, ob, a.dual, oa2, ob2, a.beta, a.C, a.ldc,
+        a.M == a.N && (a.dual || symmetric_operand(a)));
   }
 
   CUtensorMap ta, tb;
