@@ -47,3 +47,31 @@ def test_last_error_is_empty_string_initially():
         pytest.skip("libgbpoly.so not built")
     lib = gbpoly.load_library()
     assert isinstance(lib.gbpoly_last_error(), bytes)
+
+
+def test_workspace_query_is_host_logic():
+    # gbpoly_workspace_query needs no context or device: the split panels of
+    # the tensor-core forms, and the K-split partials of small FP32 grids
+    import ctypes as ct
+
+    import gbpoly
+    from gbpoly import Precision
+
+    if not gbpoly.LIB_PATH.exists():
+        pytest.skip("libgbpoly.so not built")
+    lib = gbpoly.load_library()
+
+    def query(prec, M, N, K, same=0):
+        out = ct.c_size_t()
+        assert lib.gbpoly_workspace_query(int(prec), M, N, K, same, ct.byref(out)) == 0
+        return out.value
+
+    # bf16x3: two BF16 terms of A and B, K rounded up to 64
+    assert query(Precision.BF16X3, 1000, 500, 100) >= 2 * (1000 + 500) * 128 * 2
+    assert query(Precision.BF16X3, 1000, 1000, 100, same=1) < query(Precision.BF16X3, 1000, 1000, 100)
+    # fp32: nothing for grids that fill a device, partial products for small ones
+    assert query(Precision.FP32, 8192, 8192, 8192) == 0
+    small = query(Precision.FP32, 1024, 1024, 1024)
+    assert small > 0 and small % (1024 * 1024 * 4) == 0
+    assert query(Precision.FP32, 1024, 1024, 16) == 0  # too little K to split
+    assert lib.gbpoly_workspace_query(int(Precision.FP32), -1, 4, 4, 0, ct.byref(ct.c_size_t())) != 0
