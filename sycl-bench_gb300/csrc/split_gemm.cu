@@ -90,7 +90,10 @@ struct Form {
   // FP32 registers, round to nearest, by the epilogue warps.  Two chunk
   // buffers in TMEM so the MMAs run ahead of the epilogue.
   static constexpr int CH = 128 / ROW;
-  static constexpr uint32_t TMEM_COLS = 2 * BN;
+  // TMEM allocations are powers of two (>= 32 columns); the two chunk
+  // buffers start at column 0 and TMEM_COLS / 2
+  static constexpr uint32_t TMEM_COLS = 2 * BN <= 64 ? 64 : (2 * BN <= 128 ? 128 : (2 * BN <= 256 ? 256 : 512));
+  static constexpr uint32_t BUF_COLS = TMEM_COLS / 2;
   static constexpr int HALF = BN / 2;  // columns per epilogue warp
   // Square tiles: symmetric updates compute the lower triangle of tiles and
   // mirror them.
@@ -521,7 +524,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             break;
           }
           umma::fence_after_sync();
-          const uint32_t d = tmem + uint32_t(b * F::BN);
+          const uint32_t d = tmem + uint32_t(b) * F::BUF_COLS;
           const uint32_t a_base = smem_u32(smem + s * F::STAGE);
           const uint32_t b_base = a_base + F::terms * F::A_TILE;
           // Issue order: every cross product (p >= 1) of the stage first, the
@@ -596,7 +599,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           break;
         }
         umma::fence_after_sync();
-        const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b * F::BN + h * F::HALF);
+        const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
         float sc = 1.f;  // block scale of this chunk (E4M3): left row block x right column block
         if constexpr(F::scaled) {
           const int pair = c % ti.npair, kb = c / ti.npair;
