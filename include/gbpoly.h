@@ -135,6 +135,13 @@ gbpoly_status gbpoly_autotune_gemm(gbpoly_ctx* ctx, gbpoly_precision prec, int64
  * driver version (entries of other devices in the file are kept). */
 gbpoly_status gbpoly_autotune_save(gbpoly_ctx* ctx, const char* path);
 gbpoly_status gbpoly_autotune_load(gbpoly_ctx* ctx, const char* path, int* loaded);
+/* K-split tail (CTA-pair configurations, on by default): when the last round
+ * of 256 x 256 tiles would leave at least half the resident SM pairs idle,
+ * each tile of that round runs as two halves of its K range on two pairs;
+ * the first half adds the second half's partial sums (in a fixed order, so
+ * results are the same on every run) and writes C.  The workspace query
+ * includes the partial sums. */
+gbpoly_status gbpoly_tail_split_enable(gbpoly_ctx* ctx, int enable);
 
 /* ----------------------------------------------------------------- graphs -- */
 

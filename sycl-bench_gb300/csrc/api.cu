@@ -261,6 +261,12 @@ gbpoly_status gbpoly_profile_enable(gbpoly_ctx* ctx, int enable) {
   return GBPOLY_OK;
 }
 
+gbpoly_status gbpoly_tail_split_enable(gbpoly_ctx* ctx, int enable) {
+  if(!ctx) return fail(GBPOLY_ERR_INVALID, "null context");
+  ctx->tail_split = enable != 0;
+  return GBPOLY_OK;
+}
+
 gbpoly_status gbpoly_profile_read(gbpoly_ctx* ctx, int max_entries, char* names, int* counts, double* total_ms,
     int* n_entries) {
   CTX_TRY(ctx);

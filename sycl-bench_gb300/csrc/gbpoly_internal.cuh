@@ -31,6 +31,7 @@ enum DeviceError : int {
   kDevErrMmaWait = 3,     // epilogue waited too long for the accumulator
   kDevErrDrainWait = 4,   // teardown waited too long for in-flight copies
   kDevErrTmemAlloc = 5,   // tensor-memory allocation did not fit
+  kDevErrSplitWait = 6,   // a K-split tile's first half waited too long for the second
 };
 
 struct Workspace {
@@ -67,6 +68,7 @@ struct gbpoly_ctx {
   gbpoly::Workspace stats;  // per-chunk column partial sums (colstats.cu)
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
   bool profiling = false;
+  bool tail_split = true;  // K-split units for the last round of CTA-pair tiles
   std::vector<gbpoly::ProfileRecord> prof;        // launches since the last read
   std::vector<cudaEvent_t> event_pool;            // reusable events
   // tile configuration per (form, log2-bucket of M, N, K), from the autotuner
@@ -237,6 +239,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
       return false;
     }
   }
+}
+
+// Wait until the global counter reaches `target` (other CTAs of the same
+// launch add to it).  Bounded like mbar_wait; ordered before the caller's
+// later loads on success.
+__device__ __forceinline__ bool wait_count(const int* counter, int target, int* err, int code) {
+  const volatile int* c = counter;
+  const uint64_t t0 = global_timer_ns();
+  for(int n = 0; *c < target; ++n) {
+    __nanosleep(128);
+    if((n & 15) == 15) {
+      if(*reinterpret_cast<volatile int*>(err) != 0) return false;
+      if(global_timer_ns() - t0 > kWaitTimeoutNs) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
+    }
+  }
+  __threadfence();
+  return true;
 }
 
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {

@@ -365,9 +365,31 @@ struct SingleSched {
   // only tiles on or below the diagonal are computed; the ones below it also
   // store their transpose.
   bool lower = false;
+  // Split tail (CTA pairs): when the last round of tiles would leave half the
+  // clusters or more idle, each of its tiles becomes two units of half the
+  // K iterations each, run by two clusters in that round.  The second half
+  // (role 2, iterations [split_it, end)) stores its sums in partial[slot]
+  // and counts its epilogue warps in flags[slot]; the first half (role 1,
+  // [0, split_it)) waits for all of them (bounded), adds them to its own
+  // sums and writes C.  units == 0: one unit per tile.
+  int units = 0, full_tiles = 0, split_it = 0;
+  float* partial = nullptr;  // [slot][CTA of the pair][epilogue warp][HALF / 4][32 lanes] float4
+  int* flags = nullptr;      // [slot], zero at launch
   __device__ int count() const {
     const int tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
     return lower ? tm * (tm + 1) / 2 : tm * tn;
+  }
+  __device__ int unit_count() const { return units ? units : count(); }
+  // unit u -> tile, role (0 whole tile, 1 first K half, 2 second K half),
+  // tail slot.  The half that stores its sums takes the lower unit (and
+  // cluster) index of the two, the half that waits for them the higher.
+  __device__ void unit(int u, int& t, int& role, int& slot) const {
+    if(units == 0 || u < full_tiles) {
+      t = u, role = 0, slot = 0;
+      return;
+    }
+    const int v = u - full_tiles;
+    t = full_tiles + v / 2, role = 2 - (v & 1), slot = v / 2;
   }
   __device__ TileInfo tile(int t) const {
     int tm, tn;
@@ -399,6 +421,11 @@ struct GroupedSched {
   const int4* tiles;        // (problem, tile_m, tile_n, 0)
   int ntiles;
   __device__ int count() const { return ntiles; }
+  __device__ int unit_count() const { return ntiles; }
+  int split_it = 0;
+  float* partial = nullptr;
+  int* flags = nullptr;
+  __device__ void unit(int u, int& t, int& role, int& slot) const { t = u, role = 0, slot = 0; }
   __device__ TileInfo tile(int t) const {
     const int4 e = tiles[t];
     const GroupProblem p = probs[e.x];
@@ -420,7 +447,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   float(*epi_stage)[33] = reinterpret_cast<float(*)[33]>(smem + F::STAGES * F::STAGE + 256);  // 8 warps x [32][33]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles = sched.count();
+  const int units = sched.unit_count();
   // CTA pairs: tiles are walked per cluster; rank 0 issues the MMAs and owns
   // the stage barriers, both CTAs load their halves and run the epilogue on
   // their 128 rows.
@@ -463,11 +490,14 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       // ---------------------------------------------------------- producer
       int g = 0;  // global stage iteration across tiles
       bool ok = true;
-      for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
+      for(int u = first_tile; u < units && ok; u += tile_step) {
+        int tile, role, slot;
+        sched.unit(u, tile, role, slot);
         const TileInfo ti = sched.tile(tile);
         const int m0 = ti.m0 + int(rank) * F::BM_CTA, n0 = ti.n0 + int(rank) * F::BN_CTA, npair = ti.npair;
         const int iters = (ti.Kp / F::BK) * npair;
-        for(int it = 0; it < iters; ++it, ++g) {
+        const int it0 = role == 2 ? sched.split_it : 0, it1 = role == 1 ? sched.split_it : iters;
+        for(int it = it0; it < it1; ++it, ++g) {
           const int s = g % F::STAGES;
           if(g >= F::STAGES && !mbar_wait(&empty[s], ((g / F::STAGES) - 1) & 1, err, kDevErrEmptyWait)) {
             ok = false;
@@ -505,10 +535,13 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       // ------------------------------------------------------- MMA issue
       int g = 0, chunk = 0;
       bool ok = true;
-      for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
+      for(int u = first_tile; u < units && ok; u += tile_step) {
+        int tile, role, slot;
+        sched.unit(u, tile, role, slot);
         const TileInfo ti = sched.tile(tile);
         const int iters = (ti.Kp / F::BK) * ti.npair;
-        for(int it = 0; it < iters && ok; ++it, ++g) {
+        const int it0 = role == 2 ? sched.split_it : 0, it1 = role == 1 ? sched.split_it : iters;
+        for(int it = it0; it < it1 && ok; ++it, ++g) {
           const int b = chunk & 1;
           if(it % F::CH == 0) {
             // the epilogue must have drained this chunk buffer (used two chunks ago)
@@ -557,7 +590,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             umma::commit_pair(&empty[s], 0x3);
           else
             umma::commit(&empty[s]);
-          if(it % F::CH == F::CH - 1 || it == iters - 1) {
+          if(it % F::CH == F::CH - 1 || it == it1 - 1) {
             // chunk complete in TMEM buffer b
             if constexpr(F::CG == 2)
               umma::commit_pair(&chunk_full[b], 0x3);
@@ -585,12 +618,16 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     // chunk buffers are released on the first CTA's barrier (MMAs are issued there)
     const uint32_t chunk_empty_pair[2] = {F::CG == 2 ? cluster_map(&chunk_empty[0], 0) : 0u,
         F::CG == 2 ? cluster_map(&chunk_empty[1], 0) : 0u};
-    for(int tile = first_tile; tile < tiles && ok; tile += tile_step) {
+    for(int u = first_tile; u < units && ok; u += tile_step) {
+      int tile, role, slot;
+      sched.unit(u, tile, role, slot);
       const TileInfo ti = sched.tile(tile);
       const int M = ti.M, N = ti.N;
       const float alpha = ti.alpha, beta = ti.beta;
       const int64_t ldc = ti.ldc;
-      const int chunks = ((ti.Kp / F::BK) * ti.npair + F::CH - 1) / F::CH;
+      const int iters = (ti.Kp / F::BK) * ti.npair;
+      const int it0 = role == 2 ? sched.split_it : 0, it1 = role == 1 ? sched.split_it : iters;
+      const int chunks = (it1 - it0 + F::CH - 1) / F::CH;
       const int nbase = ti.n0 + h * F::HALF;
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk & 1;
@@ -605,7 +642,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           const int pair = c % ti.npair, kb = c / ti.npair;
           const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
           const float* sr = pair ? ti.sr[1] : ti.sr[0];
-          sc = sl[(ti.m0 >> 7) * ti.kt + kb] * sr[((ti.n0 + h * F::HALF) >> 7) * ti.kt + kb];
+          sc = sl[(ti.m0 >> 7) * ti.kt + kb] * sr[(nbase >> 7) * ti.kt + kb];
         }
 #pragma unroll
         for(int j = 0; j < F::HALF / 32; ++j) {
@@ -628,6 +665,30 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
       }
       if(!ok) continue;
+      if(role != 0) {
+        // K-split tile: the second half stores its sums, the first half adds
+        // them to its own (in this order) and writes C
+        float4* part = reinterpret_cast<float4*>(sched.partial) +
+                       ((size_t(slot) * F::CG + rank) * 8 + size_t(warp - 4)) * (32 * F::HALF / 4);
+        if(role == 2) {
+#pragma unroll
+          for(int j = 0; j < F::HALF / 4; ++j)
+            __stcg(&part[j * 32 + lane], make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]));
+          __threadfence();
+          __syncwarp();
+          if(lane == 0) atomicAdd(&sched.flags[slot], 1);
+          continue;
+        }
+        if(!wait_count(&sched.flags[slot], 8 * F::CG, err, kDevErrSplitWait)) {
+          ok = false;
+          continue;
+        }
+#pragma unroll
+        for(int j = 0; j < F::HALF / 4; ++j) {
+          const float4 v = __ldcg(&part[j * 32 + lane]);
+          acc[4 * j] += v.x, acc[4 * j + 1] += v.y, acc[4 * j + 2] += v.z, acc[4 * j + 3] += v.w;
+        }
+      }
       // Write C through a per-warp 32 x 32 staging tile: each lane holds one
       // row of the block, the stores go out one 128-byte row segment per
       // instruction (coalesced for any ldc and alignment).
@@ -738,51 +799,132 @@ gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, i
   return GBPOLY_OK;
 }
 
-// Launch the tensor-core kernel for scheduler S: one persistent CTA per SM.
+// One-time per device: shared-memory opt-in and the register check of the
+// warp split.
 template <class F, class S>
-gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t tiles, const char* kernel_name) {
+gbpoly_status tc_prepare(gbpoly_ctx* ctx) {
   static unsigned attr_set = 0;
-  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
-    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
-    // setmaxnreg redistributes the registers the CTA was launched with: the
-    // split must fit in threads x registers-per-thread at launch, or the
-    // increase would wait forever.
-    cudaFuncAttributes fa;
-    GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F, S>));
-    const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
-    if(long(fa.numRegs) * F::THREADS < need)
-      return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
-    attr_set |= 1u << ctx->device;
-  }
-  if(tiles <= 0) return GBPOLY_OK;
-  if constexpr(F::CG == 2) {
-    // CTA pairs: a cluster of two per tile, as many clusters as fit at once
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
+  if(ctx->device < 32 && (attr_set & (1u << ctx->device))) return GBPOLY_OK;
+  GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
+  // setmaxnreg redistributes the registers the CTA was launched with: the
+  // split must fit in threads x registers-per-thread at launch, or the
+  // increase would wait forever.
+  cudaFuncAttributes fa;
+  GBPOLY_CUDA_TRY(cudaFuncGetAttributes(&fa, split_gemm_kernel<F, S>));
+  const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
+  if(long(fa.numRegs) * F::THREADS < need)
+    return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
+  if(ctx->device < 32) attr_set |= 1u << ctx->device;
+  return GBPOLY_OK;
+}
+
+// Launch configuration of a CTA-pair kernel: clusters of two along x.
+template <class F>
+struct PairLaunch {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  PairLaunch(gbpoly_ctx* ctx, int clusters) {
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 2;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(2 * clusters);
     cfg.blockDim = dim3(F::THREADS);
     cfg.dynamicSmemBytes = F::SMEM;
     cfg.stream = ctx->stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    static int max_clusters[32] = {};
-    if(ctx->device >= 32 || max_clusters[ctx->device] == 0) {
-      cfg.gridDim = dim3(2 * (ctx->sm_count / 2));
-      int n = 0;
-      GBPOLY_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, split_gemm_kernel<F, S>, &cfg));
-      if(n <= 0) return fail(GBPOLY_ERR_UNSUPPORTED, "no CTA pair of this tensor-core configuration fits on the device");
-      if(ctx->device < 32) max_clusters[ctx->device] = n;
-    }
-    const int clusters = int(std::min<int64_t>(tiles, ctx->device < 32 ? max_clusters[ctx->device] : 1));
-    cfg.gridDim = dim3(2 * clusters);
-    ProfileScope prof(ctx, kernel_name);
-    GBPOLY_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_gemm_kernel<F, S>, sched, ctx->err_dev));
+  }
+};
+
+// CTA pairs of configuration F resident at once on the device (cached).
+template <class F, class S>
+gbpoly_status pair_clusters(gbpoly_ctx* ctx, int& clusters) {
+  static int max_clusters[32] = {};
+  gbpoly_status st = tc_prepare<F, S>(ctx);
+  if(st != GBPOLY_OK) return st;
+  if(ctx->device < 32 && max_clusters[ctx->device] > 0) {
+    clusters = max_clusters[ctx->device];
     return GBPOLY_OK;
   }
-  const int grid = int(std::min<int64_t>(tiles, ctx->sm_count));
+  PairLaunch<F> pl(ctx, ctx->sm_count / 2);
+  int n = 0;
+  GBPOLY_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, split_gemm_kernel<F, S>, &pl.cfg));
+  if(n <= 0) return fail(GBPOLY_ERR_UNSUPPORTED, "no CTA pair of this tensor-core configuration fits on the device");
+  if(ctx->device < 32) max_clusters[ctx->device] = n;
+  clusters = n;
+  return GBPOLY_OK;
+}
+
+// K-split tail of a CTA-pair launch.  When the last round of tiles would
+// leave half the resident pairs or more idle, each of its `slots` tiles runs
+// as two units of half the K chunks; `bytes` of workspace hold their partial
+// sums and arrival counters.  Only launches of fewer than kTailMaxRounds
+// full rounds split: with more, the last round is a small share of the time
+// and pairing two clusters on one tile (the first half waits for the second)
+// costs about what it saves (measured on GB300: +6 to +15% at 2560 and 4096,
+// -1 to -3% at 8192).
+struct TailPlan {
+  int64_t units = 0;  // work units of the launch
+  int full_tiles = 0, split_it = 0, slots = 0;
+  size_t bytes = 0;
+};
+constexpr size_t kTailSlotBytes = size_t(256) * 256 * sizeof(float);  // one 256 x 256 FP32 tile
+constexpr int kTailMaxRounds = 8;
+
+template <class F, class S>
+gbpoly_status plan_tail(gbpoly_ctx* ctx, int64_t tiles, int64_t iters, TailPlan& tp) {
+  tp = TailPlan{};
+  tp.units = tiles;
+  if constexpr(F::CG == 2) {
+    static_assert(size_t(F::BM) * F::BN * sizeof(float) == kTailSlotBytes, "tail slot size");
+    const int64_t chunks = (iters + F::CH - 1) / F::CH;
+    if(!ctx->tail_split || tiles <= 0 || chunks < 2) return GBPOLY_OK;
+    int P = 0;
+    gbpoly_status st = pair_clusters<F, S>(ctx, P);
+    if(st != GBPOLY_OK) return st;
+    const int64_t R = tiles % P;
+    if(R > 0 && 2 * R <= P && tiles / P < kTailMaxRounds) {
+      tp.full_tiles = int(tiles - R);
+      tp.units = tiles + R;
+      tp.split_it = int(chunks / 2 * F::CH);
+      tp.slots = int(R);
+      tp.bytes = size_t(R) * kTailSlotBytes + align_up(size_t(R) * sizeof(int), 256);
+    }
+  }
+  return GBPOLY_OK;
+}
+
+// Point the scheduler at the tail's workspace (at `base`) and clear its counters.
+template <class S>
+gbpoly_status apply_tail(gbpoly_ctx* ctx, const TailPlan& tp, char* base, S& sched) {
+  if(tp.slots == 0) return GBPOLY_OK;
+  sched.units = int(tp.units);
+  sched.full_tiles = tp.full_tiles;
+  sched.split_it = tp.split_it;
+  sched.partial = reinterpret_cast<float*>(base);
+  sched.flags = reinterpret_cast<int*>(base + size_t(tp.slots) * kTailSlotBytes);
+  GBPOLY_CUDA_TRY(cudaMemsetAsync(sched.flags, 0, size_t(tp.slots) * sizeof(int), ctx->stream));
+  return GBPOLY_OK;
+}
+
+// Launch the tensor-core kernel for scheduler S: one persistent CTA (or CTA
+// pair) per SM (pair of SMs), walking `units` work units.
+template <class F, class S>
+gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t units, const char* kernel_name) {
+  gbpoly_status st = tc_prepare<F, S>(ctx);
+  if(st != GBPOLY_OK) return st;
+  if(units <= 0) return GBPOLY_OK;
+  if constexpr(F::CG == 2) {
+    // CTA pairs: a cluster of two per tile, as many clusters as fit at once
+    int P = 0;
+    if((st = pair_clusters<F, S>(ctx, P)) != GBPOLY_OK) return st;
+    PairLaunch<F> pl(ctx, int(std::min<int64_t>(units, P)));
+    ProfileScope prof(ctx, kernel_name);
+    GBPOLY_CUDA_TRY(cudaLaunchKernelEx(&pl.cfg, split_gemm_kernel<F, S>, sched, ctx->err_dev));
+    return GBPOLY_OK;
+  }
+  const int grid = int(std::min<int64_t>(units, ctx->sm_count));
   ProfileScope prof(ctx, kernel_name);
   split_gemm_kernel<F, S><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(sched, ctx->err_dev);
   GBPOLY_CUDA_TRY(cudaGetLastError());
@@ -819,8 +961,17 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   const Layout lay = layout<F>(a.M, a.N, a.K, same);
   const int64_t Kp = lay.Kp;
   const size_t a_stride = lay.a_stride, b_stride = lay.b_stride, a_bytes = lay.a_bytes, b_bytes = lay.b_bytes;
-  gbpoly_status st = ensure_workspace(ctx, a_bytes + b_bytes);
+  using Sched = SingleSched<F::BM, F::BN>;
+  int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
+  const bool lower = F::MIRROR && (same || a.dual) && a.M == a.N;  // symmetric product: lower triangle of tiles
+  if(lower) {
+    const int64_t t = (a.M + F::BM - 1) / F::BM;
+    tiles = t * (t + 1) / 2;
+  }
+  TailPlan tail;
+  gbpoly_status st = plan_tail<F, Sched>(ctx, tiles, (Kp / F::BK) * (a.dual ? 2 : 1), tail);
   if(st != GBPOLY_OK) return st;
+  if((st = ensure_workspace(ctx, a_bytes + b_bytes + tail.bytes)) != GBPOLY_OK) return st;
   char* ws = static_cast<char*>(ctx->ws.ptr);
   Panels pa{ws, a_stride};
   Panels pb = same ? pa : Panels{ws + a_bytes, b_stride};
@@ -842,14 +993,10 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
     maps.p[1] = maps.p[0];
   }
 
-  SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
-  int64_t tiles = ((a.M + F::BM - 1) / F::BM) * ((a.N + F::BN - 1) / F::BN);
-  if(F::MIRROR && (same || a.dual) && a.M == a.N) {  // symmetric product: lower triangle of tiles
-    const int64_t t = (a.M + F::BM - 1) / F::BM;
-    sched.lower = true;
-    tiles = t * (t + 1) / 2;
-  }
-  return launch_tc_kernel<F>(ctx, sched, tiles, kernel_name);
+  Sched sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
+  sched.lower = lower;
+  if((st = apply_tail(ctx, tail, ws + a_bytes + b_bytes, sched)) != GBPOLY_OK) return st;
+  return launch_tc_kernel<F>(ctx, sched, tail.units, kernel_name);
 }
 
 // FP8 form: quantize both operands (panels + block scales), one MMA product.
@@ -915,12 +1062,17 @@ size_t bytes_of(int64_t M, int64_t N, int64_t K, bool same) {
 }  // namespace
 
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same) {
-  // the largest over the configurations of the form (they differ only in padding)
+  // The largest over the configurations of the form (they differ only in
+  // padding), plus the K-split tail of CTA-pair configurations: at most half
+  // the resident pairs of a device of up to 256 SMs, and no more than the
+  // shape's 256 x 256 tiles.
+  const int64_t slots = std::min<int64_t>(64, ((M + 255) / 256) * ((N + 255) / 256));
+  const size_t tail = size_t(slots) * kTailSlotBytes + align_up(size_t(slots) * sizeof(int), 256);
   switch(prec) {
-  case GBPOLY_PREC_TF32: return bytes_of<FormTF32>(M, N, K, same);
-  case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same);
-  case GBPOLY_PREC_TF32X3: return bytes_of<FormTF32x3>(M, N, K, same);
-  case GBPOLY_PREC_BF16X6: return bytes_of<FormBF16x6>(M, N, K, same);
+  case GBPOLY_PREC_TF32: return bytes_of<FormTF32>(M, N, K, same) + tail;
+  case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same) + tail;
+  case GBPOLY_PREC_TF32X3: return bytes_of<FormTF32x3>(M, N, K, same) + tail;
+  case GBPOLY_PREC_BF16X6: return bytes_of<FormBF16x6>(M, N, K, same) + tail;
   case GBPOLY_PREC_FP8: {
     const size_t Kp = align_up(size_t(std::max<int64_t>(K, 1)), 128), kb = Kp / 128;
     return align_up(size_t(M) * Kp, 1024) + (same ? 0 : align_up(size_t(N) * Kp, 1024)) +

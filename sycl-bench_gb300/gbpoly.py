@@ -104,6 +104,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_event_record": (ct.c_int, [_vp, _vp]),
     "gbpoly_event_elapsed_ms": (ct.c_int, [_vp, _vp, _vp, ct.POINTER(ct.c_float)]),
     "gbpoly_profile_enable": (ct.c_int, [_vp, ct.c_int]),
+    "gbpoly_tail_split_enable": (ct.c_int, [_vp, ct.c_int]),
     "gbpoly_profile_read": (ct.c_int, [_vp, ct.c_int, ct.c_char_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double),
                                        ct.POINTER(ct.c_int)]),
     "gbpoly_gemm_f32": (ct.c_int, [_vp, ct.c_int, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
@@ -322,6 +323,10 @@ class Context:
         v = ct.c_int()
         _check(self.lib.gbpoly_gemm_config_count(int(prec), ct.byref(v)))
         return v.value
+
+    def tail_split(self, enable: bool) -> None:
+        """K-split units for the last round of CTA-pair tiles (default on)."""
+        _check(self.lib.gbpoly_tail_split_enable(self.handle, 1 if enable else 0))
 
     def config_set(self, prec, M, N, K, config: int) -> None:
         _check(self.lib.gbpoly_gemm_config_set(self.handle, int(prec), M, N, K, config))

@@ -69,6 +69,9 @@ def test_workspace_query_is_host_logic():
     # bf16x3: two BF16 terms of A and B, K rounded up to 64
     assert query(Precision.BF16X3, 1000, 500, 100) >= 2 * (1000 + 500) * 128 * 2
     assert query(Precision.BF16X3, 1000, 1000, 100, same=1) < query(Precision.BF16X3, 1000, 1000, 100)
+    # CTA-pair shapes: the panels plus the partial sums of a K-split last round
+    # (up to 64 tiles of 256 x 256 FP32)
+    assert query(Precision.BF16X3, 8192, 8192, 8192) >= 2 * 2 * 8192 * 8192 * 2 + 64 * 256 * 256 * 4
     # fp32: nothing for grids that fill a device, partial products for small ones
     assert query(Precision.FP32, 8192, 8192, 8192) == 0
     small = query(Precision.FP32, 1024, 1024, 1024)

@@ -98,3 +98,70 @@ def test_pair_configuration_symmetric_updates(ctx, prec, config):
     ctx.config_set(prec, n, n, k, 0)
     ctx.free(dA)
     ctx.free(dB)
+
+
+
+def run_split_and_whole(ctx, fn):
+    """fn() twice with the K-split tail enabled, once without: (split, split again, whole)."""
+    out = [fn(), fn()]
+    ctx.tail_split(False)
+    try:
+        out.append(fn())
+    finally:
+        ctx.tail_split(True)
+    return out
+
+
+@pytest.mark.parametrize("M,N,K", [(520, 300, 333), (1024, 768, 1024), (2560, 2560, 256)])
+@pytest.mark.parametrize("prec", FORMS, ids=lambda p: p.name.lower())
+@pytest.mark.parametrize("config", PAIR_CONFIGS)
+def test_tail_split_against_fp64_and_deterministic(ctx, prec, M, N, K, config):
+    # 6 and 12 tiles (every tile split in two K halves on two CTA pairs; a
+    # ragged edge) and 100 tiles (only the last round's tiles split): within
+    # the form's bound, the same bits on every run, and close to the result
+    # of whole tiles (only the order of two partial sums differs)
+    rng = np.random.default_rng(M + N + K + config)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    C = rng.standard_normal((M, N)).astype(np.float32)
+    split, again, whole = run_split_and_whole(ctx, lambda: run_pair(ctx, prec, A, B, C, 1.25, -0.5, config=config))
+    np.testing.assert_array_equal(split.view(np.uint32), again.view(np.uint32))
+    ref = oracle.gemm_f64(A, B, C, 1.25, -0.5)
+    assert oracle.error_norms(split, ref)[1] < BOUND[prec]
+    assert oracle.error_norms(whole, ref)[1] < BOUND[prec]
+    assert np.linalg.norm(split - whole) / np.linalg.norm(whole) < 1e-6
+
+
+@pytest.mark.parametrize("config", PAIR_CONFIGS)
+def test_tail_split_symmetric_updates(ctx, config):
+    # lower triangle of 4 x 4 pair tiles (10 tiles, all K-split): the first
+    # half of a tile below the diagonal also writes its mirror
+    n, k = 1000, 300
+    rng = np.random.default_rng(11)
+    A = rng.uniform(-1, 1, (n, k)).astype(np.float32)
+    B = rng.uniform(-1, 1, (n, k)).astype(np.float32)
+    C = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    dA, dB = ctx.upload(A), ctx.upload(B)
+    ctx.config_set(Precision.BF16X3, n, n, k, config)
+
+    def run(name):
+        dC = ctx.upload(C)
+        if name == "syrk":
+            ctx.syrk(Precision.BF16X3, n, k, 1.5, dA, k, -0.5, dC, n)
+        else:
+            ctx.syr2k(Precision.BF16X3, n, k, 1.5, dA, k, dB, k, -0.5, dC, n)
+        ctx.synchronize()
+        out = ctx.download(dC, C.shape)
+        ctx.free(dC)
+        return out
+
+    refs = {"syrk": oracle.gemm_f64(A, A, C, 1.5, -0.5, op_b=1),
+            "syr2k": oracle.gemm_f64(A, B, C, 1.5, -0.5, op_b=1, A2=B, B2=A)}
+    for name in ("syrk", "syr2k"):
+        split, again, whole = run_split_and_whole(ctx, lambda: run(name))
+        np.testing.assert_array_equal(split.view(np.uint32), again.view(np.uint32), err_msg=name)
+        assert oracle.error_norms(split, refs[name])[1] < BOUND[Precision.BF16X3], name
+        assert np.linalg.norm(split - whole) / np.linalg.norm(whole) < 1e-6, name
+    ctx.config_set(Precision.BF16X3, n, n, k, 0)
+    ctx.free(dA)
+    ctx.free(dB)
