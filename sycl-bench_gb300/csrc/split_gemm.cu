@@ -163,73 +163,114 @@ struct Term<Elem::TF32> {
 };
 
 // ------------------------------------------------------------- split pass --
-// panel[t][r][k] (r < R, k < Kp) = term t of op(X)[r][k] for k < K, 0 beyond,
-// op(X)[r][k] = X[r*ld + k] (k_major) or X[k*ld + r].  Panels are Kp-strided
-// and `panel_stride` elements apart.
-template <Elem E, int TERMS>
-__device__ __forceinline__ void split_tile(const float* __restrict__ X, int64_t ld, int k_major, int R, int K, int Kp,
-    typename Term<E>::T* __restrict__ out, int64_t panel_stride, int64_t r0, int64_t k0, float (*tile)[65]) {
-  using T = typename Term<E>::T;
+// One 64 x 64 block of op(X) at (r0, k0) in three steps, so that a
+// persistent loop can issue the next block's loads before converting the
+// current one:
+//   split_load:    the block into 16 registers per thread (256 threads),
+//                  coalesced along X's contiguous dimension; 128-bit loads
+//                  when the block is whole and aligned (returns true then);
+//   split_stage:   the registers into the shared tile [r][k];
+//   split_convert: the tile's rows into the term panels.
+__device__ __forceinline__ bool split_load(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
+    int64_t r0, int64_t k0, float (&v)[16]) {
   const int tid = threadIdx.x;
-  // Load the 64 x 64 block of op(X) into shared memory, coalesced along X's
-  // contiguous dimension; 128-bit loads when the block is whole and aligned.
   const int64_t r_lim = R - r0, k_lim = K - k0;
+  const int64_t o0 = k_major ? r0 : k0, i0 = k_major ? k0 : r0;  // outer (strided) and inner (contiguous) origin
   const bool whole = r_lim >= 64 && k_lim >= 64 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
-  // (all of a thread's loads are issued before its shared-memory stores)
   if(whole) {
-    float4 v[4];
+    // float4 e of the thread: outer index tid / 16 + 16 e, inner 4 (tid % 16)
+    const float* p = X + (o0 + (tid >> 4)) * ld + i0 + 4 * (tid & 15);
 #pragma unroll
     for(int e = 0; e < 4; ++e) {
-      const int idx = tid + e * 256;  // 0..1023 float4 of the block
-      const int outer = idx >> 4, inner = (idx & 15) * 4;
-      v[e] = k_major ? *reinterpret_cast<const float4*>(X + (r0 + outer) * ld + k0 + inner)   // read along k
-                     : *reinterpret_cast<const float4*>(X + (k0 + outer) * ld + r0 + inner);  // read along r
-    }
-#pragma unroll
-    for(int e = 0; e < 4; ++e) {
-      const int idx = tid + e * 256;
-      const int outer = idx >> 4, inner = (idx & 15) * 4;
-      if(k_major) {
-        tile[outer][inner] = v[e].x;
-        tile[outer][inner + 1] = v[e].y;
-        tile[outer][inner + 2] = v[e].z;
-        tile[outer][inner + 3] = v[e].w;
-      } else {
-        tile[inner][outer] = v[e].x;
-        tile[inner + 1][outer] = v[e].y;
-        tile[inner + 2][outer] = v[e].z;
-        tile[inner + 3][outer] = v[e].w;
-      }
+      const float4 x = *reinterpret_cast<const float4*>(p + e * 16 * ld);
+      v[4 * e] = x.x, v[4 * e + 1] = x.y, v[4 * e + 2] = x.z, v[4 * e + 3] = x.w;
     }
   } else {
-    float v[16];
+    // element e of the thread: outer index tid / 64 + 4 e, inner tid % 64
+    const int in = tid & 63, out = tid >> 6;
+    const bool in_ok = in < (k_major ? k_lim : r_lim);
+    const int64_t out_lim = k_major ? r_lim : k_lim;
+    const float* p = X + (o0 + out) * ld + i0 + in;
+#pragma unroll
+    for(int e = 0; e < 16; ++e) v[e] = (in_ok && out + 4 * e < out_lim) ? p[e * 4 * ld] : 0.f;
+  }
+  return whole;
+}
+
+__device__ __forceinline__ void split_stage(bool whole, int k_major, const float (&v)[16], float (*tile)[65]) {
+  const int tid = threadIdx.x;
+  if(whole) {
+    const int out = tid >> 4, in = 4 * (tid & 15);
+#pragma unroll
+    for(int e = 0; e < 4; ++e)
+#pragma unroll
+      for(int q = 0; q < 4; ++q) {
+        if(k_major)
+          tile[out + 16 * e][in + q] = v[4 * e + q];
+        else
+          tile[in + q][out + 16 * e] = v[4 * e + q];
+      }
+  } else {
+    const int in = tid & 63, out = tid >> 6;
 #pragma unroll
     for(int e = 0; e < 16; ++e) {
-      const int idx = tid + e * 256;
-      const int rr = k_major ? (idx >> 6) : (idx & 63);
-      const int kk = k_major ? (idx & 63) : (idx >> 6);
-      v[e] = (rr < r_lim && kk < k_lim) ? (k_major ? X[(r0 + rr) * ld + k0 + kk] : X[(k0 + kk) * ld + r0 + rr]) : 0.f;
-    }
-#pragma unroll
-    for(int e = 0; e < 16; ++e) {
-      const int idx = tid + e * 256;
-      tile[k_major ? (idx >> 6) : (idx & 63)][k_major ? (idx & 63) : (idx >> 6)] = v[e];
+      if(k_major)
+        tile[out + 4 * e][in] = v[e];
+      else
+        tile[in][out + 4 * e] = v[e];
     }
   }
-  __syncthreads();
+}
+
+// Terms of 16 consecutive values: t[j] = round(x - t[0] - ... - t[j-1]).
+// BF16: two values per conversion (cvt.rn.bf16x2.f32, the same round to
+// nearest even as one at a time).
+template <Elem E, int TERMS>
+struct SplitTerms {
+  using T = typename Term<E>::T;
+  __device__ static void run(const float* x, T (&t)[TERMS][16]) {
+#pragma unroll
+    for(int i = 0; i < 16; ++i) {
+      float rem = x[i];
+#pragma unroll
+      for(int j = 0; j < TERMS; ++j) {
+        t[j][i] = Term<E>::round(rem);
+        rem -= Term<E>::widen(t[j][i]);
+      }
+    }
+  }
+};
+template <int TERMS>
+struct SplitTerms<Elem::BF16, TERMS> {
+  __device__ static void run(const float* x, __nv_bfloat16 (&t)[TERMS][16]) {
+#pragma unroll
+    for(int i = 0; i < 16; i += 2) {
+      float a = x[i], b = x[i + 1];
+#pragma unroll
+      for(int j = 0; j < TERMS; ++j) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        t[j][i] = h.x;
+        t[j][i + 1] = h.y;
+        a -= __low2float(h);
+        b -= __high2float(h);
+      }
+    }
+  }
+};
+
+template <Elem E, int TERMS>
+__device__ __forceinline__ void split_convert(const float (*tile)[65], typename Term<E>::T* __restrict__ out,
+    int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0) {
+  using T = typename Term<E>::T;
+  const int tid = threadIdx.x;
   const int rr = tid >> 2, kc = (tid & 3) * 16;
   const int64_t r = r0 + rr;
   if(r >= R) return;
+  float x[16];
+#pragma unroll
+  for(int i = 0; i < 16; ++i) x[i] = tile[rr][kc + i];
   __align__(16) T t[TERMS][16];
-#pragma unroll
-  for(int i = 0; i < 16; ++i) {
-    float rem = tile[rr][kc + i];
-#pragma unroll
-    for(int j = 0; j < TERMS; ++j) {
-      t[j][i] = Term<E>::round(rem);
-      rem -= Term<E>::widen(t[j][i]);
-    }
-  }
+  SplitTerms<E, TERMS>::run(x, t);
   constexpr int kVec = 16 * sizeof(T) / 16;  // uint4 per 16 elements
 #pragma unroll
   for(int j = 0; j < TERMS; ++j) {
@@ -239,16 +280,24 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ X, int64_t 
   }
 }
 
+// panel[t][r][k] (r < R, k < Kp) = term t of op(X)[r][k] for k < K, 0 beyond,
+// op(X)[r][k] = X[r*ld + k] (k_major) or X[k*ld + r].  Panels are Kp-strided
+// and `panel_stride` elements apart.  One 64 x 64 block per CTA.
 template <Elem E, int TERMS>
 __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
     int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride) {
   __shared__ float tile[64][65];
-  split_tile<E, TERMS>(X, ld, k_major, R, K, Kp, out, panel_stride, int64_t(blockIdx.y) * 64,
-      int64_t(blockIdx.x) * 64, tile);
+  const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
+  float v[16];
+  const bool whole = split_load(X, ld, k_major, R, K, r0, k0, v);
+  split_stage(whole, k_major, v, tile);
+  __syncthreads();
+  split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0);
 }
 
 // One operand of a grouped call: its 64x64 blocks are blocks
-// [block_start, block_start + ceil(R/64) * Kp/64) of the grouped split launch.
+// [block_start, block_start + ceil(R/64) * Kp/64) of the grouped split pass,
+// row block by row block.
 struct SplitJob {
   const float* X;
   int64_t ld;
@@ -258,17 +307,47 @@ struct SplitJob {
   int block_start, kblocks;
 };
 
-// block_job[b]: the job block b belongs to (a table written by the plan, so
-// a block starts its copy after two dependent loads rather than a search)
+// Grouped split pass: persistent CTAs walk the blocks in a grid-stride loop
+// (block b, b + gridDim.x, ...: the blocks in flight at a time are
+// neighbours in memory, as in a one-block-per-CTA launch), loading the next
+// block while converting the current one.  block_job[b] (written by the
+// plan) gives a block's job; the job index of the block after next is read
+// one iteration ahead.
 template <Elem E, int TERMS>
-__global__ void __launch_bounds__(256) grouped_split_kernel(const SplitJob* __restrict__ jobs,
-    const int* __restrict__ block_job) {
+__global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* __restrict__ jobs,
+    const int* __restrict__ block_job, int nblocks) {
+  using T = typename Term<E>::T;
   __shared__ float tile[64][65];
-  const int b = blockIdx.x;
-  const SplitJob j = jobs[block_job[b]];
-  const int local = b - j.block_start;
-  split_tile<E, TERMS>(j.X, j.ld, j.k_major, j.R, j.K, j.Kp, static_cast<typename Term<E>::T*>(j.out),
-      j.panel_stride, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, tile);
+  const int step = gridDim.x;
+  int b = blockIdx.x;
+  if(b >= nblocks) return;
+  SplitJob j = jobs[block_job[b]];
+  int ji_next = b + step < nblocks ? block_job[b + step] : 0;
+  int local = b - j.block_start;
+  float v[16];
+  bool whole = split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64,
+      int64_t(local % j.kblocks) * 64, v);
+  while(true) {
+    split_stage(whole, j.k_major, v, tile);
+    __syncthreads();
+    // the current block's job, for its conversion below
+    T* const out = static_cast<T*>(j.out);
+    const int64_t panel_stride = j.panel_stride, r0 = int64_t(local / j.kblocks) * 64,
+                  k0 = int64_t(local % j.kblocks) * 64;
+    const int R = j.R, Kp = j.Kp;
+    const int nb = b + step;
+    if(nb < nblocks) {  // next block's loads in flight during the conversion
+      j = jobs[ji_next];
+      ji_next = nb + step < nblocks ? block_job[nb + step] : 0;
+      local = nb - j.block_start;
+      whole = split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64,
+          int64_t(local % j.kblocks) * 64, v);
+    }
+    split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0);
+    if(nb >= nblocks) break;
+    b = nb;
+    __syncthreads();  // the tile is read before the next block overwrites it
+  }
 }
 
 // ---------------------------------------------------------- FP8 quantize --
@@ -1342,7 +1421,9 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
   using T = typename Term<F::elem>::T;
   if(g->split_blocks > 0) {
     ProfileScope prof(ctx, "grouped_split");
-    grouped_split_kernel<F::elem, F::terms><<<g->split_blocks, 256, 0, ctx->stream>>>(g->jobs, g->block_job);
+    // persistent: 4 CTAs per SM
+    const int ctas = std::min(g->split_blocks, 4 * std::max(1, ctx->sm_count));
+    grouped_split_kernel<F::elem, F::terms><<<ctas, 256, 0, ctx->stream>>>(g->jobs, g->block_job, g->split_blocks);
     GBPOLY_CUDA_TRY(cudaGetLastError());
   }
   (void)sizeof(T);
