@@ -452,7 +452,7 @@ struct SingleSched {
   // [0, split_it)) waits for all of them (bounded), adds them to its own
   // sums and writes C.  units == 0: one unit per tile.
   int units = 0, full_tiles = 0, split_it = 0;
-  float* partial = nullptr;  // [slot][CTA of the pair][epilogue warp][HALF / 4][32 lanes] float4
+  float* partial = nullptr;  // [slot][CTA of the pair][128 rows][BN columns]
   int* flags = nullptr;      // [slot], zero at launch
   __device__ int count() const {
     const int tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
@@ -744,28 +744,15 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
       }
       if(!ok) continue;
-      if(role != 0) {
-        // K-split tile: the second half stores its sums, the first half adds
-        // them to its own (in this order) and writes C
-        float4* part = reinterpret_cast<float4*>(sched.partial) +
-                       ((size_t(slot) * F::CG + rank) * 8 + size_t(warp - 4)) * (32 * F::HALF / 4);
-        if(role == 2) {
-#pragma unroll
-          for(int j = 0; j < F::HALF / 4; ++j)
-            __stcg(&part[j * 32 + lane], make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]));
-          __threadfence();
-          __syncwarp();
-          if(lane == 0) atomicAdd(&sched.flags[slot], 1);
-          continue;
-        }
-        if(!wait_count(&sched.flags[slot], 8 * F::CG, err, kDevErrSplitWait)) {
+      // K-split tile: the second half stores its sums (partial tile of the
+      // CTA: 128 rows x BN, row-major), the first half waits for them and
+      // adds them to its own (first + second) before writing C
+      float* part = nullptr;
+      if(F::CG == 2 && role != 0) {
+        part = sched.partial + ((size_t(slot) * F::CG + rank) * 128 + 32 * q) * F::BN + h * F::HALF + lane;
+        if(role == 1 && !wait_count(&sched.flags[slot], 8 * F::CG, err, kDevErrSplitWait)) {
           ok = false;
           continue;
-        }
-#pragma unroll
-        for(int j = 0; j < F::HALF / 4; ++j) {
-          const float4 v = __ldcg(&part[j * 32 + lane]);
-          acc[4 * j] += v.x, acc[4 * j + 1] += v.y, acc[4 * j + 2] += v.z, acc[4 * j + 3] += v.w;
         }
       }
       // Write C through a per-warp 32 x 32 staging tile: each lane holds one
@@ -778,6 +765,18 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
 #pragma unroll
         for(int i = 0; i < 32; ++i) stage[lane][i] = acc[32 * j + i];
         __syncwarp();
+        if(F::CG == 2 && role != 0) {
+          float* pj = part + 32 * j;  // column lane of this warp's 32 rows
+          if(role == 2) {
+#pragma unroll 4
+            for(int r = 0; r < 32; ++r) __stcg(pj + r * F::BN, stage[r][lane]);
+            __syncwarp();
+            continue;
+          }
+#pragma unroll 4
+          for(int r = 0; r < 32; ++r) stage[r][lane] += __ldcg(pj + r * F::BN);
+          __syncwarp();
+        }
         const int n = nbase + 32 * j + lane;
         if(n < N) {
           const int rows = min(32, M - row0);
@@ -818,6 +817,11 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           }
         }
         __syncwarp();
+      }
+      if(F::CG == 2 && role == 2) {  // sums stored: count this warp
+        __threadfence();
+        __syncwarp();
+        if(lane == 0) atomicAdd(&sched.flags[slot], 1);
       }
     }
   }
