@@ -87,13 +87,15 @@ struct Form {
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + EPI_STAGE;
   // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
   // accumulation inside the tensor core stays short); chunks are summed in
-  // FP32 registers, round to nearest, by the epilogue warps.  Two chunk
-  // buffers in TMEM so the MMAs run ahead of the epilogue.
+  // FP32 registers, round to nearest, by the epilogue warps.  NBUF chunk
+  // buffers in TMEM (all 512 columns: 2 of 256, 4 of 128) so the MMAs run
+  // ahead of the epilogue, also across the C stores between two tiles.
   static constexpr int CH = 128 / ROW;
-  // TMEM allocations are powers of two (>= 32 columns); the two chunk
-  // buffers start at column 0 and TMEM_COLS / 2
-  static constexpr uint32_t TMEM_COLS = 2 * BN <= 64 ? 64 : (2 * BN <= 128 ? 128 : (2 * BN <= 256 ? 256 : 512));
-  static constexpr uint32_t BUF_COLS = TMEM_COLS / 2;
+  static constexpr int NBUF = BN <= 128 ? 4 : 2;
+  // TMEM allocations are powers of two (>= 32 columns); chunk buffer b
+  // starts at column b * BUF_COLS
+  static constexpr uint32_t TMEM_COLS = NBUF * BN <= 64 ? 64 : (NBUF * BN <= 128 ? 128 : (NBUF * BN <= 256 ? 256 : 512));
+  static constexpr uint32_t BUF_COLS = TMEM_COLS / NBUF;
   static constexpr int HALF = BN / 2;  // columns per epilogue warp
   // Square tiles: symmetric updates compute the lower triangle of tiles and
   // mirror them.
@@ -105,7 +107,8 @@ struct Form {
   static_assert(CG == 1 || (CG == 2 && !scaled && BN % 32 == 0), "CTA pairs: BF16 and TF32 forms");
   static_assert(STAGE_TX == CG * STAGE, "pair stage bytes");
   static_assert(SMEM <= 232448, "shared memory");
-  static_assert(TMEM_COLS <= 512, "tensor memory");
+  static_assert(TMEM_COLS <= 512 && BUF_COLS >= BN, "tensor memory");
+  static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= 256, "barriers fit their 256 bytes");
 };
 
 // Tile configurations per form (index = config id).  Config 0 is the default.
@@ -519,9 +522,9 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + F::STAGES * F::STAGE);
   uint64_t* empty = full + F::STAGES;
-  uint64_t* chunk_full = empty + F::STAGES;  // [2]
-  uint64_t* chunk_empty = chunk_full + 2;    // [2]
-  uint64_t* drain = chunk_empty + 2;
+  uint64_t* chunk_full = empty + F::STAGES;     // [NBUF]
+  uint64_t* chunk_empty = chunk_full + F::NBUF;  // [NBUF]
+  uint64_t* drain = chunk_empty + F::NBUF;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   float(*epi_stage)[33] = reinterpret_cast<float(*)[33]>(smem + F::STAGES * F::STAGE + 256);  // 8 warps x [32][33]
 
@@ -539,7 +542,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for(int b = 0; b < 2; ++b) {
+    for(int b = 0; b < F::NBUF; ++b) {
       mbar_init(&chunk_full[b], 1);
       mbar_init(&chunk_empty[b], 8 * F::CG);  // one arrival per epilogue warp of the pair
     }
@@ -621,10 +624,10 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         const int iters = (ti.Kp / F::BK) * ti.npair;
         const int it0 = role == 2 ? sched.split_it : 0, it1 = role == 1 ? sched.split_it : iters;
         for(int it = it0; it < it1 && ok; ++it, ++g) {
-          const int b = chunk & 1;
+          const int b = chunk % F::NBUF;
           if(it % F::CH == 0) {
-            // the epilogue must have drained this chunk buffer (used two chunks ago)
-            if(chunk >= 2 && !mbar_wait(&chunk_empty[b], ((chunk >> 1) - 1) & 1, err, kDevErrMmaWait)) {
+            // the epilogue must have drained this chunk buffer (used NBUF chunks ago)
+            if(chunk >= F::NBUF && !mbar_wait(&chunk_empty[b], ((chunk / F::NBUF) - 1) & 1, err, kDevErrMmaWait)) {
               ok = false;
               break;
             }
@@ -695,6 +698,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     int chunk = 0;
     bool ok = true;
     // chunk buffers are released on the first CTA's barrier (MMAs are issued there)
+    static_assert(F::CG == 1 || F::NBUF == 2, "CTA pairs: two chunk buffers");
     const uint32_t chunk_empty_pair[2] = {F::CG == 2 ? cluster_map(&chunk_empty[0], 0) : 0u,
         F::CG == 2 ? cluster_map(&chunk_empty[1], 0) : 0u};
     for(int u = first_tile; u < units && ok; u += tile_step) {
@@ -709,8 +713,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       const int chunks = (it1 - it0 + F::CH - 1) / F::CH;
       const int nbase = ti.n0 + h * F::HALF;
       for(int c = 0; c < chunks; ++c, ++chunk) {
-        const int b = chunk & 1;
-        if(!mbar_wait(&chunk_full[b], (chunk >> 1) & 1, err, kDevErrMmaWait)) {
+        const int b = chunk % F::NBUF;
+        if(!mbar_wait(&chunk_full[b], (chunk / F::NBUF) & 1, err, kDevErrMmaWait)) {
           ok = false;
           break;
         }
