@@ -297,6 +297,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     grouped = None if args.no_grouped else run_grouped_workload(ctx, args)
     family = None if args.no_family else run_family(ctx, args)
     neighbours = None if args.no_neighbours else run_neighbours(ctx, args)
+    small_k = None if args.no_small_k else run_small_k(ctx, args)
 
     head = tiers[headline.name.lower()]
     peaks, peak_kind = load_peaks()
@@ -329,7 +330,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
                 "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
         "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
         "device": props, "peak_kind": peak_kind, "grouped": grouped, "family": family,
-        "neighbours": neighbours,
+        "neighbours": neighbours, "small_k": small_k,
     }
 
 
@@ -530,6 +531,60 @@ def run_family(ctx, args) -> dict:
     for k in ("2mm", "3mm", "syrk", "syr2k"):
         out[k]["speedup_bf16x3_vs_fp32"] = out[k]["bf16x3"]["tflops"] / out[k]["fp32"]["tflops"]
     out["normal01_inputs"] = "seeded normal(0, 1) A, B, C, D (numpy default_rng(4096)), same chains, alpha and beta"
+    return out
+
+
+def run_small_k(ctx, args) -> dict:
+    """GEMMs whose K is too short for the tensor or FMA pipes to bound them:
+    C = A.B + C at M = N = args.size, K in {32, 64, 128, 256, 512}, seeded
+    uniform[-1, 1] inputs, fp32 and bf16x3.  The bound is HBM: every call
+    reads and writes C (M N 8 bytes) and reads A and B ((M + N) K 4 bytes);
+    reported as those algorithmic bytes per second against the measured copy
+    bandwidth, with TFLOP/s and the per-kernel split (bf16x3: split pass and
+    tensor-core kernel)."""
+    import gbpoly
+    from gbpoly import Precision
+
+    n = args.size
+    peaks, _ = load_peaks()
+    hbm = peaks.get("hbm_gbs")
+    rng = np.random.default_rng(64)
+    dC = ctx.upload(rng.uniform(-1, 1, (n, n)).astype(np.float32))
+    out = {"m_n": n, "beta": 1.0, "bytes": "M N 8 (C read and written) + (M + N) K 4 (A, B read)"}
+    steps = max(args.steps, 5)
+    for K in (32, 64, 128, 256, 512):
+        dA = ctx.upload(rng.uniform(-1, 1, (n, K)).astype(np.float32))
+        dB = ctx.upload(rng.uniform(-1, 1, (K, n)).astype(np.float32))
+        row = {}
+        for prec in (Precision.FP32, Precision.BF16X3):
+            ctx.workspace_reserve(ctx.workspace_query(prec, n, n, K))
+
+            def step(prec=prec):
+                ctx.gemm(prec, n, n, K, 1.0, dA, K, dB, n, 1.0, dC, n)
+            for _ in range(args.warmup):
+                step()
+            ctx.synchronize()
+            e0, e1 = ctx.event(), ctx.event()
+            e0.record()
+            for _ in range(steps):
+                step()
+            e1.record()
+            ctx.synchronize()
+            ms = e0.elapsed_ms(e1) / steps
+            ctx.profile(True)
+            ctx.profile_read()
+            for _ in range(steps):
+                step()
+            kernels = {k: round(t / c * 1e3, 2) for k, (c, t) in ctx.profile_read().items()}
+            ctx.profile(False)
+            gbs = (n * n * 8 + 2 * n * K * 4) / (ms * 1e-3) / 1e9
+            row[prec.name.lower()] = {"us_per_call": ms * 1e3, "tflops": 2.0 * n * n * K / (ms * 1e-3) / 1e12,
+                                      "gbs": gbs, "frac_of_hbm": gbs / hbm if hbm else None,
+                                      "kernel_us": kernels}
+        out[f"K={K}"] = row
+        ctx.free(dA)
+        ctx.free(dB)
+    ctx.free(dC)
     return out
 
 
@@ -849,6 +904,7 @@ def main() -> None:
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-GEMM workload")
     ap.add_argument("--grouped-count", type=int, default=512)
     ap.add_argument("--no-family", action="store_true", help="skip the 2mm/3mm/syrk/syr2k section")
+    ap.add_argument("--no-small-k", action="store_true", help="skip the small-K (HBM-bound) GEMM section")
     ap.add_argument("--no-neighbours", action="store_true",
                     help="skip covariance/correlation/matmulchain/matrix-vector section")
     ap.add_argument("--forms", default="fp32,bf16x3,tf32x3,bf16x6,tf32,fp8", help="forms to time (comma list)")
@@ -902,7 +958,7 @@ def main() -> None:
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
                     peaks=res["peak_kind"], grouped=res["grouped"], family=res["family"],
-                    neighbours=res["neighbours"])
+                    neighbours=res["neighbours"], small_k=res["small_k"])
         print(json.dumps(line))
     dist.close()
 

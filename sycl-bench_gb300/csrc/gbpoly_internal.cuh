@@ -261,6 +261,11 @@ __device__ __forceinline__ bool wait_count(const int* counter, int target, int* 
   return true;
 }
 
+// Fetch the 128-byte line holding p into L2 (no register or shared-memory cost).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
