@@ -117,10 +117,13 @@ gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N
 
 /* Each tensor-core form has a few compiled tile configurations: tile width,
  * K bytes per pipeline stage, pipeline depth and cluster size (tf32, bf16x3,
- * tf32x3, bf16x6: configurations 3 and 4 run CTA pairs, cta_group::2 MMAs
- * on 256 x 256 tiles).  The context keeps one per (form, ceil(log2) of M, N,
- * K); unless tuned or set, a shape whose 256 x 256 tiles give every SM pair
- * a tile uses configuration 3, smaller ones a 128 x 128 configuration. */
+ * tf32x3, bf16x6: configurations 3, 4 and 5 run CTA pairs, cta_group::2 MMAs
+ * on 256 x 256 tiles; 5 keeps the C tile in shared memory, loaded and stored
+ * by TMA, for short K, and runs as 3 for symmetric products or C rows that
+ * are not 16-byte aligned).  The context keeps one per (form, ceil(log2) of
+ * M, N, K); unless tuned or set, a shape whose 256 x 256 tiles give every SM
+ * pair a tile uses configuration 5 up to K = 256 (tf32: 512, tf32x3: 128)
+ * and 3 beyond, smaller ones a 128 x 128 configuration. */
 gbpoly_status gbpoly_gemm_config_count(gbpoly_precision prec, int* count);
 gbpoly_status gbpoly_gemm_config_set(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K,
     int config);

@@ -66,10 +66,14 @@ constexpr uint32_t idesc_of() {
 // cta_group::2 MMAs: each CTA holds 128 rows of the A tile and BN/2 rows of
 // the B tile in its shared memory, and 128 rows x BN columns of the
 // accumulator in its TMEM.
-template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128, int CG_ = 1>
+// CEPI_: the C tile of a CTA (128 x BN FP32) has its own shared-memory
+// buffer, filled by TMA when the tile starts and written back by TMA stores
+// (non-symmetric products with 16-byte-aligned C rows; no K-split tail).
+template <Elem E, int TERMS, int NPROD, int BN_, int STAGES_, int ROW_ = 128, int CG_ = 1, bool CEPI_ = false>
 struct Form {
   static constexpr Elem elem = E;
   static constexpr int CG = CG_;
+  static constexpr bool CEPI = CEPI_;
   static constexpr int terms = TERMS, nprod = NPROD, BN = BN_, STAGES = STAGES_;
   static constexpr int BM_CTA = 128, BM = BM_CTA * CG;   // rows per CTA; rows of a (pair) tile
   static constexpr int BN_CTA = BN / CG;                 // B rows staged per CTA
@@ -84,7 +88,10 @@ struct Form {
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);  // bytes per stage in each CTA
   static constexpr int STAGE_TX = CG * STAGE;              // bytes a stage's barrier waits for (both CTAs)
   static constexpr int EPI_STAGE = 8 * 32 * 33 * 4;  // epilogue staging, one 32x33 fp32 tile per warp
-  static constexpr int SMEM = STAGES * STAGE + 1024 + 256 + EPI_STAGE;
+  static constexpr int C_BOX = 32 * 32 * 4;          // CEPI: one 32 x 32 FP32 box of C (128-byte swizzle)
+  static constexpr int C_TILE = 8 * (BN / 64) * C_BOX;  // CEPI: 8 epilogue warps x HALF / 32 boxes
+  // stages, barriers (256 bytes; CEPI: padded to 1 KB), epilogue staging or the C tile, alignment slack
+  static constexpr int SMEM = CEPI ? STAGES * STAGE + 1024 + C_TILE + 1024 : STAGES * STAGE + 1024 + 256 + EPI_STAGE;
   // Accumulation: CH stage iterations per TMEM chunk (round-toward-zero
   // accumulation inside the tensor core stays short); chunks are summed in
   // FP32 registers, round to nearest, by the epilogue warps.  NBUF chunk
@@ -108,7 +115,8 @@ struct Form {
   static_assert(STAGE_TX == CG * STAGE, "pair stage bytes");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert(TMEM_COLS <= 512 && BUF_COLS >= BN, "tensor memory");
-  static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= 256, "barriers fit their 256 bytes");
+  static_assert((2 * STAGES + 2 * NBUF + 1 + (CEPI ? 8 : 0)) * 8 + 4 <= 256, "barriers fit their 256 bytes");
+  static_assert(!CEPI || (ROW == 128 && !scaled && CG == 2), "C-tile epilogue: CTA-pair 128-byte-row forms");
 };
 
 // Tile configurations per form (index = config id).  Config 0 is the default.
@@ -135,6 +143,12 @@ using FormTF32_q = Form<Elem::TF32, 1, 1, 256, 12, 64, 2>;
 using FormBF16x3_q = Form<Elem::BF16, 2, 3, 256, 6, 64, 2>;
 using FormTF32x3_q = Form<Elem::TF32, 2, 3, 256, 6, 64, 2>;
 using FormBF16x6_q = Form<Elem::BF16, 3, 6, 256, 4, 64, 2>;
+// CTA pairs with the C tile in shared memory (TMA loads and stores of C,
+// fewer pipeline stages): GEMMs whose K is too short to hide C's traffic
+using FormTF32_t = Form<Elem::TF32, 1, 1, 256, 2, 128, 2, true>;
+using FormBF16x3_t = Form<Elem::BF16, 2, 3, 256, 1, 128, 2, true>;
+using FormTF32x3_t = Form<Elem::TF32, 2, 3, 256, 1, 128, 2, true>;
+using FormBF16x6_t = Form<Elem::BF16, 3, 6, 256, 1, 128, 2, true>;
 
 // Term indices of product p: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 ? 1 : (p == 4 ? 1 : (p == 5 ? 2 : 0)); }
@@ -457,6 +471,7 @@ struct SingleSched {
   int units = 0, full_tiles = 0, split_it = 0;
   float* partial = nullptr;  // [slot][CTA of the pair][128 rows][BN columns]
   int* flags = nullptr;      // [slot], zero at launch
+  CUtensorMap cmap;          // C-tile epilogue forms: C (M x N, boxes of 32 x 32, 128-byte swizzle)
   __device__ int count() const {
     const int tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
     return lower ? tm * (tm + 1) / 2 : tm * tn;
@@ -539,7 +554,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
   uint64_t* chunk_full = empty + F::STAGES;     // [NBUF]
   uint64_t* chunk_empty = chunk_full + F::NBUF;  // [NBUF]
   uint64_t* drain = chunk_empty + F::NBUF;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  uint64_t* cbar = drain + 1;  // C-tile epilogue: one barrier per epilogue warp for its C boxes
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1 + (F::CEPI ? 8 : 0));
   float(*epi_stage)[33] = reinterpret_cast<float(*)[33]>(smem + F::STAGES * F::STAGE + 256);  // 8 warps x [32][33]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -561,6 +577,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       mbar_init(&chunk_empty[b], 8 * F::CG);  // one arrival per epilogue warp of the pair
     }
     mbar_init(drain, 1);
+    if constexpr(F::CEPI)
+      for(int w = 0; w < 8; ++w) mbar_init(&cbar[w], 1);
     fence_mbar_init();
   }
   if(warp == 1) {
@@ -711,6 +729,9 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
     float acc[F::HALF];
     int chunk = 0;
     bool ok = true;
+    // C-tile epilogue: this warp's HALF / 32 boxes of C, loads and stores issued so far
+    char* const cbox = smem + F::STAGES * F::STAGE + 1024 + (warp - 4) * (F::HALF / 32) * F::C_BOX;
+    int c_loads = 0, c_stores = 0;
     // chunk buffers are released on the first CTA's barrier (MMAs are issued there)
     static_assert(F::CG == 1 || F::NBUF == 2, "CTA pairs: two chunk buffers");
     const uint32_t chunk_empty_pair[2] = {F::CG == 2 ? cluster_map(&chunk_empty[0], 0) : 0u,
@@ -726,13 +747,28 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       const int it0 = role == 2 ? sched.split_it : 0, it1 = role == 1 ? sched.split_it : iters;
       const int chunks = (it1 - it0 + F::CH - 1) / F::CH;
       const int nbase = ti.n0 + h * F::HALF;
+      const int crow = ti.m0 + int(rank) * F::BM_CTA + 32 * q;
+      if constexpr(F::CEPI) {
+        // this tile's C into the warp's boxes while the MMAs run (once the
+        // previous tile's stores have read them)
+        if(beta != 0.f) {
+          if(lane == 0) {
+            if(c_stores > 0) bulk_wait_read_all();
+            mbar_arrive_expect_tx(&cbar[warp - 4], (F::HALF / 32) * F::C_BOX);
+#pragma unroll
+            for(int j = 0; j < F::HALF / 32; ++j)
+              tma_load_2d(cbox + j * F::C_BOX, &sched.cmap, &cbar[warp - 4], nbase + 32 * j, crow);
+          }
+          ++c_loads;
+        }
+      }
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk % F::NBUF;
         // C under this warp's 32 rows x HALF columns (and their mirror) into
         // L2 a few chunks before the tile's end, ahead of the epilogue's
         // loads (prefetching the next tile's C a whole epilogue ahead was
         // slower: 178 -> 190 us at M = N = 8192, K = 64)
-        if(c == max(0, chunks - 4) && beta != 0.f && role != 2) prefetch_c_warp<F>(ti, rank, q, h, lane);
+        if(!F::CEPI && c == max(0, chunks - 4) && beta != 0.f && role != 2) prefetch_c_warp<F>(ti, rank, q, h, lane);
         if(!mbar_wait(&chunk_full[b], (chunk / F::NBUF) & 1, err, kDevErrMmaWait)) {
           ok = false;
           break;
@@ -767,6 +803,44 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
       }
       if(!ok) continue;
+      if constexpr(F::CEPI) {
+        // C = alpha acc + beta C in the boxes (lane = row: eight 16-byte
+        // chunks, swizzled by row, so each quarter warp covers all banks),
+        // then TMA stores (clipped at the matrix edges)
+        if(beta != 0.f) {
+          if(!mbar_wait(&cbar[warp - 4], (c_loads - 1) & 1, err, kDevErrMmaWait)) {
+            ok = false;
+            continue;
+          }
+        } else {
+          if(lane == 0 && c_stores > 0) bulk_wait_read_all();
+          __syncwarp();
+        }
+#pragma unroll
+        for(int j = 0; j < F::HALF / 32; ++j) {
+          char* row = cbox + j * F::C_BOX + lane * 128;
+#pragma unroll
+          for(int k = 0; k < 8; ++k) {
+            float4* p4 = reinterpret_cast<float4*>(row + ((k ^ (lane & 7)) << 4));
+            const float4 cv = beta != 0.f ? *p4 : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 o;
+            o.x = fmaf(beta, cv.x, alpha * acc[32 * j + 4 * k]);
+            o.y = fmaf(beta, cv.y, alpha * acc[32 * j + 4 * k + 1]);
+            o.z = fmaf(beta, cv.z, alpha * acc[32 * j + 4 * k + 2]);
+            o.w = fmaf(beta, cv.w, alpha * acc[32 * j + 4 * k + 3]);
+            *p4 = o;
+          }
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if(lane == 0) {
+#pragma unroll
+          for(int j = 0; j < F::HALF / 32; ++j) tma_store_2d(&sched.cmap, cbox + j * F::C_BOX, nbase + 32 * j, crow);
+          bulk_commit();
+        }
+        ++c_stores;
+        continue;
+      }
       // K-split tile: the second half stores its sums (partial tile of the
       // CTA: 128 rows x BN, row-major), the first half waits for them and
       // adds them to its own (first + second) before writing C
@@ -847,6 +921,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         if(lane == 0) atomicAdd(&sched.flags[slot], 1);
       }
     }
+    if constexpr(F::CEPI)
+      if(lane == 0 && c_stores > 0) bulk_wait_all();  // C written before the CTA leaves
   }
 
   umma::fence_before_sync();
@@ -982,7 +1058,7 @@ template <class F, class S>
 gbpoly_status plan_tail(gbpoly_ctx* ctx, int64_t tiles, int64_t iters, TailPlan& tp) {
   tp = TailPlan{};
   tp.units = tiles;
-  if constexpr(F::CG == 2) {
+  if constexpr(F::CG == 2 && !F::CEPI) {
     static_assert(size_t(F::BM) * F::BN * sizeof(float) == kTailSlotBytes, "tail slot size");
     const int64_t chunks = (iters + F::CH - 1) / F::CH;
     if(!ctx->tail_split || tiles <= 0 || chunks < 2) return GBPOLY_OK;
@@ -1058,6 +1134,11 @@ Layout layout(int64_t M, int64_t N, int64_t K, bool same) {
 // syrk: both operands are the rows of A; split once
 bool same_operand(const GemmF32Args& a) { return symmetric_operand(a); }
 
+// C rows that TMA can load and store: 16-byte-aligned base and row pitch.
+bool c_tile_ok(const GemmF32Args& a) {
+  return (reinterpret_cast<uintptr_t>(a.C) & 15) == 0 && (a.ldc & 3) == 0;
+}
+
 template <class F>
 gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel_name) {
   if(a.M == 0 || a.N == 0) return GBPOLY_OK;
@@ -1101,6 +1182,12 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
 
   Sched sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
   sched.lower = lower;
+  if constexpr(F::CEPI) {
+    if(lower || !c_tile_ok(a)) return fail(GBPOLY_ERR_UNSUPPORTED, "C-tile epilogue: non-symmetric, 16-byte-aligned C");
+    if((st = make_tmap_2d(ctx, &sched.cmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.C, a.M, a.N, a.ldc, 32, 32,
+            CU_TENSOR_MAP_SWIZZLE_128B)) != GBPOLY_OK)
+      return st;
+  }
   if((st = apply_tail(ctx, tail, ws + a_bytes + b_bytes, sched)) != GBPOLY_OK) return st;
   return launch_tc_kernel<F>(ctx, sched, tail.units, kernel_name);
 }
@@ -1196,7 +1283,7 @@ int tensor_config_count(gbpoly_precision prec) {
   case GBPOLY_PREC_TF32:
   case GBPOLY_PREC_BF16X3:
   case GBPOLY_PREC_TF32X3:
-  case GBPOLY_PREC_BF16X6: return 5;  // configurations 3, 4: CTA pairs
+  case GBPOLY_PREC_BF16X6: return 6;  // configurations 3, 4, 5: CTA pairs (5: C tile in shared memory)
   case GBPOLY_PREC_FP8: return 1;
   default: return 0;
   }
@@ -1209,21 +1296,25 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   case GBPOLY_PREC_TF32 * 8 + 2: return run_form<FormTF32_c>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 3: return run_form<FormTF32_p>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 4: return run_form<FormTF32_q>(ctx, a, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 5: return run_form<FormTF32_t>(ctx, a, "tf32_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form<FormBF16x3>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form<FormBF16x3_b>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form<FormBF16x3_c>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 3: return run_form<FormBF16x3_p>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 4: return run_form<FormBF16x3_q>(ctx, a, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 5: return run_form<FormBF16x3_t>(ctx, a, "bf16x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form<FormTF32x3>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form<FormTF32x3_b>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form<FormTF32x3_c>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 3: return run_form<FormTF32x3_p>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 4: return run_form<FormTF32x3_q>(ctx, a, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 5: return run_form<FormTF32x3_t>(ctx, a, "tf32x3_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form<FormBF16x6>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form<FormBF16x6_b>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form<FormBF16x6_c>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 3: return run_form<FormBF16x6_p>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form<FormBF16x6_q>(ctx, a, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 5: return run_form<FormBF16x6_t>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
@@ -1278,10 +1369,17 @@ int square_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N) {
 }  // namespace
 
 // Configuration of an untuned shape: CTA pairs (256 x 256 tiles) when they
-// fill the device, else the 1-CTA configuration with the most tiles.
-int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t) {
+// fill the device, with the C tile in shared memory (configuration 5) while
+// K is short enough that C's traffic bounds the call (measured on GB300 at
+// M = N = 8192: 1.75x faster up to K = 128, ahead up to K = 256 for the
+// BF16 forms and K = 512 for tf32, behind beyond), else the 1-CTA
+// configuration with the most tiles.
+int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K) {
   if(prec == GBPOLY_PREC_FP8 || tensor_config_count(prec) <= 3) return 0;
-  if(pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256))) return 3;
+  if(pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256))) {
+    const int64_t k_tile = prec == GBPOLY_PREC_TF32 ? 512 : (prec == GBPOLY_PREC_TF32X3 ? 128 : 256);
+    return K <= k_tile ? 5 : 3;
+  }
   // 128 x 128 tiles: configuration 2 (0 for bf16x6, whose configuration 0 is 128 x 128)
   return prec == GBPOLY_PREC_BF16X6 ? 0 : 2;
 }
@@ -1300,22 +1398,26 @@ gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const G
   case GBPOLY_PREC_TF32 * 8 + 0: return run_form_panel<FormTF32>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 1: return run_form_panel<FormTF32_b>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 2: return run_form_panel<FormTF32_c>(ctx, a, plan.M, first, r0, "tf32_gemm");
-  case GBPOLY_PREC_TF32 * 8 + 3: return run_form_panel<FormTF32_p>(ctx, a, plan.M, first, r0, "tf32_gemm");
+  case GBPOLY_PREC_TF32 * 8 + 3:
+  case GBPOLY_PREC_TF32 * 8 + 5: return run_form_panel<FormTF32_p>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_TF32 * 8 + 4: return run_form_panel<FormTF32_q>(ctx, a, plan.M, first, r0, "tf32_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 0: return run_form_panel<FormBF16x3>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 1: return run_form_panel<FormBF16x3_b>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 2: return run_form_panel<FormBF16x3_c>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
-  case GBPOLY_PREC_BF16X3 * 8 + 3: return run_form_panel<FormBF16x3_p>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
+  case GBPOLY_PREC_BF16X3 * 8 + 3:
+  case GBPOLY_PREC_BF16X3 * 8 + 5: return run_form_panel<FormBF16x3_p>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_BF16X3 * 8 + 4: return run_form_panel<FormBF16x3_q>(ctx, a, plan.M, first, r0, "bf16x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 0: return run_form_panel<FormTF32x3>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 1: return run_form_panel<FormTF32x3_b>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 2: return run_form_panel<FormTF32x3_c>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
-  case GBPOLY_PREC_TF32X3 * 8 + 3: return run_form_panel<FormTF32x3_p>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
+  case GBPOLY_PREC_TF32X3 * 8 + 3:
+  case GBPOLY_PREC_TF32X3 * 8 + 5: return run_form_panel<FormTF32x3_p>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_TF32X3 * 8 + 4: return run_form_panel<FormTF32x3_q>(ctx, a, plan.M, first, r0, "tf32x3_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 0: return run_form_panel<FormBF16x6>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 1: return run_form_panel<FormBF16x6_b>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 2: return run_form_panel<FormBF16x6_c>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
-  case GBPOLY_PREC_BF16X6 * 8 + 3: return run_form_panel<FormBF16x6_p>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
+  case GBPOLY_PREC_BF16X6 * 8 + 3:
+  case GBPOLY_PREC_BF16X6 * 8 + 5: return run_form_panel<FormBF16x6_p>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form_panel<FormBF16x6_q>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);  // quantises both operands per panel
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
@@ -1326,6 +1428,7 @@ gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const G
   int config = tuned_config(ctx, prec, a.M, a.N, a.K);
   const bool symmetric = (same_operand(a) || a.dual) && a.M == a.N;
   if(symmetric && !config_is_square(prec, config)) config = square_config(ctx, prec, a.N);
+  if(config == 5 && !c_tile_ok(a)) config = 3;  // C rows TMA cannot address: the staged epilogue
   return launch_gemm_tensor_config(ctx, prec, config, a);
 }
 

@@ -1,6 +1,7 @@
 """CTA-pair (cluster of two, cta_group::2) configurations of the tensor-core
-forms, through the C ABI: configurations 3 (128-byte rows) and 4 (64-byte
-rows, deeper pipeline) of tf32, bf16x3, tf32x3 and bf16x6 compute 256 x 256
+forms, through the C ABI: configurations 3 (128-byte rows), 4 (64-byte
+rows, deeper pipeline) and 5 (C tile in shared memory, TMA loads and stores
+of C) of tf32, bf16x3, tf32x3 and bf16x6 compute 256 x 256
 tiles with each CTA holding half of the A and B tiles.  Results against FP64 within each form's bound (the same bounds as
 the other configurations), on shapes that leave the second CTA of a pair
 beyond the last row, walk several tiles per cluster, and use one or many
@@ -165,3 +166,57 @@ def test_tail_split_symmetric_updates(ctx, config):
     ctx.config_set(Precision.BF16X3, n, n, k, 0)
     ctx.free(dA)
     ctx.free(dB)
+
+
+@pytest.mark.parametrize("M,N,K", [(256, 256, 64), (300, 520, 70), (1024, 768, 32), (1000, 1000, 512)])
+@pytest.mark.parametrize("prec", FORMS, ids=lambda p: p.name.lower())
+@pytest.mark.parametrize("beta", [0.0, -0.5])
+def test_c_tile_epilogue_is_bitwise_the_staged_one(ctx, prec, M, N, K, beta):
+    # configuration 5 (C tile in shared memory, TMA loads and stores of C)
+    # computes every element as configuration 3 does: alpha acc + beta C,
+    # the same chunk sums; ragged edges are clipped by the TMA stores
+    rng = np.random.default_rng(M * 3 + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    C = rng.standard_normal((M, N)).astype(np.float32)
+    ctx.tail_split(False)  # configuration 5 has no K-split tail: compare whole tiles
+    try:
+        staged = run_pair(ctx, prec, A, B, C, 1.25, beta, config=3)
+        tiled = run_pair(ctx, prec, A, B, C, 1.25, beta, config=5)
+    finally:
+        ctx.tail_split(True)
+    np.testing.assert_array_equal(tiled.view(np.uint32), staged.view(np.uint32))
+    assert oracle.error_norms(tiled, oracle.gemm_f64(A, B, C, 1.25, beta))[1] < BOUND[prec]
+
+
+def test_c_tile_epilogue_falls_back_for_unaligned_c_and_symmetric_products(ctx):
+    # C rows TMA cannot address (ldc not a multiple of 4 floats) and syrk run
+    # the staged epilogue when configuration 5 is set for their shape
+    M, N, K = 520, 301, 96
+    rng = np.random.default_rng(17)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)  # ldc = 301
+    got = run_pair(ctx, Precision.BF16X3, A, B, C, 1.0, 0.5, config=5)
+    assert oracle.error_norms(got, oracle.gemm_f64(A, B, C, 1.0, 0.5))[1] < BOUND[Precision.BF16X3]
+    n, k = 1000, 96
+    X = rng.uniform(-1, 1, (n, k)).astype(np.float32)
+    C2 = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    dX, dC = ctx.upload(X), ctx.upload(C2)
+    ctx.config_set(Precision.BF16X3, n, n, k, 5)
+    ctx.syrk(Precision.BF16X3, n, k, 1.5, dX, k, -0.5, dC, n)
+    ctx.synchronize()
+    ctx.config_set(Precision.BF16X3, n, n, k, 0)
+    ref = oracle.gemm_f64(X, X, C2, 1.5, -0.5, op_b=1)
+    assert oracle.error_norms(ctx.download(dC, C2.shape), ref)[1] < BOUND[Precision.BF16X3]
+    ctx.free(dX)
+    ctx.free(dC)
+
+
+def test_default_configuration_by_k(ctx):
+    # pair-filling shapes: the C-tile configuration while K is short, the
+    # staged one beyond; small grids keep a 128 x 128 configuration
+    assert ctx.config_get(Precision.BF16X3, 8192, 8192, 64) == 5
+    assert ctx.config_get(Precision.BF16X3, 8192, 8192, 8192) == 3
+    assert ctx.config_get(Precision.TF32, 8192, 8192, 512) == 5
+    assert ctx.config_get(Precision.BF16X3, 512, 512, 64) not in (3, 4, 5)
