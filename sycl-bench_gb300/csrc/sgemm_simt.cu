@@ -213,6 +213,16 @@ __global__ void __launch_bounds__(kThreads, 1) sgemm_tma_kernel(const __grid_con
 
   bool ok = true;
   for(int kt = 0; kt < nkt; ++kt) {
+    if(kt == max(0, nkt - 4) && beta != 0.f) {
+      // C of the tile (and of its mirror) into L2 a few k tiles before the
+      // epilogue reads it: 512 lines of 128 bytes, two per consumer thread
+#pragma unroll
+      for(int e = 0; e < 2; ++e) {
+        const int line = tid + kConsumers * e, r = line >> 2, c = 32 * (line & 3);
+        if(m0 + r < M && n0 + c < N) prefetch_l2(C + int64_t(m0 + r) * ldc + n0 + c);
+        if(mirror && n0 + r < N && m0 + c < M) prefetch_l2(C + int64_t(n0 + r) * ldc + m0 + c);
+      }
+    }
     const int s = kt % STAGES;
     if(!mbar_wait(&full[s], (kt / STAGES) & 1, err, kDevErrFullWait)) {
       ok = false;
