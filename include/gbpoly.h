@@ -120,7 +120,7 @@ gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N
  * tf32x3, bf16x6: configurations 3, 4 and 5 run CTA pairs, cta_group::2 MMAs
  * on 256 x 256 tiles; 5 keeps the C tile in shared memory, loaded and stored
  * by TMA, for short K, and runs as 3 for symmetric products or C rows that
- * are not 16-byte aligned).  The context keeps one per (form, ceil(log2) of
+ * do not start and end on 16-byte boundaries).  The context keeps one per (form, ceil(log2) of
  * M, N, K); unless tuned or set, a shape whose 256 x 256 tiles give every SM
  * pair a tile uses configuration 5 up to K = 256 (tf32: 512, tf32x3: 128)
  * and 3 beyond, smaller ones a 128 x 128 configuration. */

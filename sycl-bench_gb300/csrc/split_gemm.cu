@@ -1134,9 +1134,11 @@ Layout layout(int64_t M, int64_t N, int64_t K, bool same) {
 // syrk: both operands are the rows of A; split once
 bool same_operand(const GemmF32Args& a) { return symmetric_operand(a); }
 
-// C rows that TMA can load and store: 16-byte-aligned base and row pitch.
+// C rows that TMA can load and store: 16-byte-aligned base and row pitch, and
+// rows ending on a 16-byte boundary (TMA stores clip the row end at 16-byte
+// granularity: a ragged N would write into the padding of ldc).
 bool c_tile_ok(const GemmF32Args& a) {
-  return (reinterpret_cast<uintptr_t>(a.C) & 15) == 0 && (a.ldc & 3) == 0;
+  return (reinterpret_cast<uintptr_t>(a.C) & 15) == 0 && (a.ldc & 3) == 0 && (a.N & 3) == 0;
 }
 
 template <class F>

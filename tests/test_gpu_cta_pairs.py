@@ -220,3 +220,26 @@ def test_default_configuration_by_k(ctx):
     assert ctx.config_get(Precision.BF16X3, 8192, 8192, 8192) == 3
     assert ctx.config_get(Precision.TF32, 8192, 8192, 512) == 5
     assert ctx.config_get(Precision.BF16X3, 512, 512, 64) not in (3, 4, 5)
+
+
+@pytest.mark.parametrize("N,ldc", [(90, 96), (300, 304), (256, 260)])
+def test_c_tile_epilogue_leaves_the_padding_of_ldc(ctx, N, ldc):
+    # configuration 5 set for the shape: rows that end inside a 16-byte chunk
+    # (N not a multiple of 4) take the staged epilogue; the padding columns
+    # of C keep their values either way
+    M, K = 300, 64
+    rng = np.random.default_rng(N + ldc)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    Cp = rng.uniform(-1, 1, (M, ldc)).astype(np.float32)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(Cp)
+    ctx.config_set(Precision.BF16X3, M, N, K, 5)
+    ctx.gemm(Precision.BF16X3, M, N, K, 1.0, dA, K, dB, N, 0.5, dC, ldc)
+    ctx.synchronize()
+    ctx.config_set(Precision.BF16X3, M, N, K, 0)
+    out = ctx.download(dC, Cp.shape)
+    np.testing.assert_array_equal(out[:, N:], Cp[:, N:])
+    ref = oracle.gemm_f64(A, B, np.ascontiguousarray(Cp[:, :N]), 1.0, 0.5)
+    assert oracle.error_norms(np.ascontiguousarray(out[:, :N]), ref)[1] < BOUND[Precision.BF16X3]
+    for b in (dA, dB, dC):
+        ctx.free(b)

@@ -174,3 +174,17 @@ def test_invalid_arguments_are_rejected(ctx):
         ctx.gemm(P, 4, 4, 4, 1.0, buf, 2, buf, 4, 0.0, buf, 4)  # lda < K
     assert e.value.status == gbpoly.Status.INVALID
     ctx.synchronize()
+
+
+@pytest.mark.parametrize("N,ldc", [(96, 104), (90, 100), (128, 132)])
+def test_gemm_leaves_the_padding_of_ldc(ctx, N, ldc):
+    # row ends on and off 16-byte boundaries: the padding keeps its values
+    rng = np.random.default_rng(N * ldc)
+    M, K = 150, 70
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    Cp = rng.uniform(-1, 1, (M, ldc)).astype(np.float32)
+    out = run_gemm(ctx, A, B, Cp, 1.0, 1.0, ldc=ldc)
+    np.testing.assert_array_equal(out[:, N:], Cp[:, N:])
+    ref = oracle.gemm_f64(A, B, np.ascontiguousarray(Cp[:, :N]), 1.0, 1.0)
+    assert oracle.error_norms(np.ascontiguousarray(out[:, :N]), ref)[1] < 1e-5
