@@ -862,6 +862,45 @@ def run_grouped_workload(ctx, args) -> dict:
             ctx.graph_destroy(graph)
         ctx.grouped_destroy(plan)
     out["speedup_bf16x3_vs_fp32"] = out["bf16x3"]["tflops"] / out["fp32"]["tflops"]
+
+    # the members HBM bounds: K <= 128 (C read and written per call against 2 M N K
+    # FLOPs), as a grouped plan of their own against their per-GEMM FP32 launches
+    sub = [i for i, (M, N, K) in enumerate(shapes) if K <= 128]
+    sub_bytes = float(sum(4 * (M * K + K * N + 2 * M * N) for M, N, K in (shapes[i] for i in sub)))
+    peaks, _ = load_peaks()
+    hbm = peaks.get("hbm_gbs")
+    small = {"count": len(sub), "bytes_per_step": sub_bytes,
+             "bytes": "sum of 4 (M K + K N + 2 M N): A, B read, C read and written"}
+    sub_descs = ctx.descs([items[i] for i in sub])
+    for prec in (Precision.FP32, Precision.BF16X3):
+        plan = ctx.grouped_plan(prec, sub_descs)
+        graph = None
+        if prec != Precision.FP32:
+            ctx.graph_begin()
+            ctx.grouped_run(plan)
+            graph = ctx.graph_end()
+
+        def sub_step():
+            if graph is not None:
+                ctx.graph_launch(graph)
+            else:
+                ctx.grouped_run(plan)
+        for _ in range(args.warmup):
+            sub_step()
+        ctx.synchronize()
+        e0, e1 = ctx.event(), ctx.event()
+        e0.record()
+        for _ in range(args.steps):
+            sub_step()
+        e1.record()
+        ctx.synchronize()
+        ms = e0.elapsed_ms(e1) / args.steps
+        gbs = sub_bytes / (ms * 1e-3) / 1e9
+        small[prec.name.lower()] = {"ms_per_step": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm if hbm else None}
+        if graph is not None:
+            ctx.graph_destroy(graph)
+        ctx.grouped_destroy(plan)
+    out["small_k_members"] = small
     for r in refs:
         ctx.free(r)
     for _, dA, dB, dC in mats:
