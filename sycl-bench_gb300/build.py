@@ -15,7 +15,7 @@ finds them under bin/benchmarks/<name>.
 
 Translation units compile in parallel; a unit is rebuilt only when it or a
 header it may include is newer than its object.  Host code is portable C++17
-(the GPU machine is aarch64, this build also runs on x86_64).
+(Grace hosts are aarch64; the same sources build on x86_64).
 """
 from __future__ import annotations
 
