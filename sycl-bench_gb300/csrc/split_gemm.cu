@@ -378,16 +378,49 @@ __global__ void __launch_bounds__(256) quantize_e4m3_kernel(const float* __restr
   __shared__ float red[8];
   const int tid = threadIdx.x;
   const int64_t r0 = int64_t(blockIdx.y) * 128, k0 = int64_t(blockIdx.x) * 128;
+  const int64_t o0 = k_major ? r0 : k0, i0 = k_major ? k0 : r0;  // outer (strided) and inner (contiguous) origin
+  const bool whole = R - r0 >= 128 && K - k0 >= 128 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
   float amax = 0.f;
-  for(int e = 0; e < 64; ++e) {
-    const int idx = tid + e * 256;  // 0..16383
-    const int rr = k_major ? (idx >> 7) : (idx & 127);
-    const int kk = k_major ? (idx & 127) : (idx >> 7);
-    const int64_t r = r0 + rr, k = k0 + kk;
-    float v = 0.f;
-    if(r < R && k < K) v = k_major ? X[r * ld + k] : X[k * ld + r];
-    blk[rr * 129 + kk] = v;
-    amax = fmaxf(amax, fabsf(v));
+  if(whole) {
+    // float4 e of the thread: outer index tid / 32 + 8 e, inner 4 (tid % 32);
+    // all 16 loads in flight before the shared-memory stores
+    const int out = tid >> 5, in = 4 * (tid & 31);
+    const float* p = X + (o0 + out) * ld + i0 + in;
+    float4 v[16];
+#pragma unroll
+    for(int e = 0; e < 16; ++e) v[e] = *reinterpret_cast<const float4*>(p + int64_t(e) * 8 * ld);
+    // store j of a float4 writes its element (j + lane / 8) % 4: the warp's
+    // 32 words then fall in 32 different banks (row stride 129)
+    const int rot = (tid >> 3) & 3;
+#pragma unroll
+    for(int e = 0; e < 16; ++e) {
+      const int o = out + 8 * e;
+      amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v[e].x), fabsf(v[e].y)), fmaxf(fabsf(v[e].z), fabsf(v[e].w))));
+#pragma unroll
+      for(int j = 0; j < 4; ++j) {
+        const int q = (j + rot) & 3;
+        const float xq = q == 0 ? v[e].x : (q == 1 ? v[e].y : (q == 2 ? v[e].z : v[e].w));
+        blk[k_major ? o * 129 + in + q : (in + q) * 129 + o] = xq;
+      }
+    }
+  } else {
+    // element e of the thread: outer index tid / 128 + 2 e, inner tid % 128
+    const int out = tid >> 7, in = tid & 127;
+    const int64_t in_lim = k_major ? K - k0 : R - r0, out_lim = k_major ? R - r0 : K - k0;
+    const float* p = X + (o0 + out) * ld + i0 + in;
+#pragma unroll
+    for(int b = 0; b < 64; b += 16) {
+      float v[16];
+#pragma unroll
+      for(int e = 0; e < 16; ++e)
+        v[e] = (in < in_lim && out + 2 * (b + e) < out_lim) ? p[int64_t(b + e) * 2 * ld] : 0.f;
+#pragma unroll
+      for(int e = 0; e < 16; ++e) {
+        const int o = out + 2 * (b + e);
+        blk[k_major ? o * 129 + in : in * 129 + o] = v[e];
+        amax = fmaxf(amax, fabsf(v[e]));
+      }
+    }
   }
 #pragma unroll
   for(int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
@@ -399,13 +432,16 @@ __global__ void __launch_bounds__(256) quantize_e4m3_kernel(const float* __restr
   const float scale = m > 0.f ? m / 448.f : 1.f;
   const float inv = 1.f / scale;
   if(tid == 0) scales[int64_t(blockIdx.y) * (Kp / 128) + blockIdx.x] = scale;
-  // each thread: one row, 64 consecutive k (two threads per row)
+  // each thread: one row, 64 consecutive k (two threads per row), two values
+  // per conversion (round to nearest, saturating, as one at a time)
   const int rr = tid >> 1, kc = (tid & 1) * 64;
   const int64_t r = r0 + rr;
   if(r >= R) return;
-  __align__(16) __nv_fp8_storage_t q[64];
+  __align__(16) __nv_fp8x2_storage_t q[32];
 #pragma unroll
-  for(int i = 0; i < 64; ++i) q[i] = __nv_cvt_float_to_fp8(blk[rr * 129 + kc + i] * inv, __NV_SATFINITE, __NV_E4M3);
+  for(int i = 0; i < 32; ++i)
+    q[i] = __nv_cvt_float2_to_fp8x2(make_float2(blk[rr * 129 + kc + 2 * i] * inv, blk[rr * 129 + kc + 2 * i + 1] * inv),
+        __NV_SATFINITE, __NV_E4M3);
   uint4* dst = reinterpret_cast<uint4*>(out + r * Kp + k0 + kc);
 #pragma unroll
   for(int v = 0; v < 4; ++v) dst[v] = reinterpret_cast<const uint4*>(q)[v];
