@@ -798,6 +798,17 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           ++c_loads;
         }
       }
+      // E4M3: the block scales of chunk c + 1 are loaded while chunk c is
+      // waited for and summed (their global-memory latency off the chunk's path)
+      auto chunk_scale = [&](int cc) -> float {
+        const int pair = cc % ti.npair, kb = cc / ti.npair;
+        const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
+        const float* sr = pair ? ti.sr[1] : ti.sr[0];
+        return sl[(ti.m0 >> 7) * ti.kt + kb] * sr[(nbase >> 7) * ti.kt + kb];
+      };
+      float sc_next = 1.f;
+      if constexpr(F::scaled)
+        if(chunks > 0) sc_next = chunk_scale(0);
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk % F::NBUF;
         // C under this warp's 32 rows x HALF columns (and their mirror) into
@@ -813,10 +824,8 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
         float sc = 1.f;  // block scale of this chunk (E4M3): left row block x right column block
         if constexpr(F::scaled) {
-          const int pair = c % ti.npair, kb = c / ti.npair;
-          const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
-          const float* sr = pair ? ti.sr[1] : ti.sr[0];
-          sc = sl[(ti.m0 >> 7) * ti.kt + kb] * sr[(nbase >> 7) * ti.kt + kb];
+          sc = sc_next;
+          if(c + 1 < chunks) sc_next = chunk_scale(c + 1);
         }
 #pragma unroll
         for(int j = 0; j < F::HALF / 32; ++j) {
