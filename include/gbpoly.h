@@ -123,7 +123,9 @@ gbpoly_status gbpoly_workspace_query(gbpoly_precision prec, int64_t M, int64_t N
  * do not start and end on 16-byte boundaries).  The context keeps one per (form, ceil(log2) of
  * M, N, K); unless tuned or set, a shape whose 256 x 256 tiles give every SM
  * pair a tile uses configuration 5 up to K = 256 (tf32: 512, tf32x3: 128)
- * and 3 beyond, smaller ones a 128 x 128 configuration. */
+ * and 3 beyond, smaller ones a 128 x 128 configuration.  fp8: configuration
+ * 1 (128 x 256 tiles) when its tiles give every SM one, else 0 (128 x 128,
+ * also every symmetric product). */
 gbpoly_status gbpoly_gemm_config_count(gbpoly_precision prec, int* count);
 gbpoly_status gbpoly_gemm_config_set(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K,
     int config);

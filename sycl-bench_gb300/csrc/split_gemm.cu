@@ -133,6 +133,7 @@ using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
 using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
 using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 2, 64>;
 using FormFP8 = Form<Elem::E4M3, 1, 1, 128, 6>;
+using FormFP8_w = Form<Elem::E4M3, 1, 1, 256, 4>;  // 128 x 256 tiles: twice the MMA work per scaled chunk
 // CTA-pair configurations (cluster of 2, 256 x 256 tiles)
 using FormTF32_p = Form<Elem::TF32, 1, 1, 256, 6, 128, 2>;
 using FormBF16x3_p = Form<Elem::BF16, 2, 3, 256, 3, 128, 2>;
@@ -1240,8 +1241,8 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
 }
 
 // FP8 form: quantize both operands (panels + block scales), one MMA product.
+template <class F>
 gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
-  using F = FormFP8;
   if(a.M == 0 || a.N == 0) return GBPOLY_OK;
   if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
     return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");
@@ -1331,7 +1332,7 @@ int tensor_config_count(gbpoly_precision prec) {
   case GBPOLY_PREC_BF16X3:
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6: return 6;  // configurations 3, 4, 5: CTA pairs (5: C tile in shared memory)
-  case GBPOLY_PREC_FP8: return 1;
+  case GBPOLY_PREC_FP8: return 2;  // configuration 1: 128 x 256 tiles
   default: return 0;
   }
 }
@@ -1362,7 +1363,8 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   case GBPOLY_PREC_BF16X6 * 8 + 3: return run_form<FormBF16x6_p>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form<FormBF16x6_q>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 5: return run_form<FormBF16x6_t>(ctx, a, "bf16x6_gemm");
-  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);
+  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8<FormFP8>(ctx, a);
+  case GBPOLY_PREC_FP8 * 8 + 1: return run_fp8<FormFP8_w>(ctx, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
 }
@@ -1401,7 +1403,7 @@ bool config_is_square(gbpoly_precision prec, int config) {
   case GBPOLY_PREC_BF16X3:
   case GBPOLY_PREC_TF32X3: return config == 2 || config == 3 || config == 4;
   case GBPOLY_PREC_BF16X6: return config == 0 || config == 1 || config == 3 || config == 4;
-  case GBPOLY_PREC_FP8: return true;
+  case GBPOLY_PREC_FP8: return config == 0;
   default: return false;
   }
 }
@@ -1422,7 +1424,10 @@ int square_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N) {
 // BF16 forms and K = 512 for tf32, behind beyond), else the 1-CTA
 // configuration with the most tiles.
 int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K) {
-  if(prec == GBPOLY_PREC_FP8 || tensor_config_count(prec) <= 3) return 0;
+  // fp8: 128 x 256 tiles (twice the MMA work per scaled chunk: 1.38x at
+  // N = 8192) when they give every SM a tile, else 128 x 128
+  if(prec == GBPOLY_PREC_FP8) return ((M + 127) / 128) * ((N + 255) / 256) >= ctx->sm_count ? 1 : 0;
+  if(tensor_config_count(prec) <= 3) return 0;
   if(pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256))) {
     const int64_t k_tile = prec == GBPOLY_PREC_TF32 ? 512 : (prec == GBPOLY_PREC_TF32X3 ? 128 : 256);
     return K <= k_tile ? 5 : 3;
@@ -1466,7 +1471,8 @@ gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const G
   case GBPOLY_PREC_BF16X6 * 8 + 3:
   case GBPOLY_PREC_BF16X6 * 8 + 5: return run_form_panel<FormBF16x6_p>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form_panel<FormBF16x6_q>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
-  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8(ctx, a);  // quantises both operands per panel
+  case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8<FormFP8>(ctx, a);  // quantises both operands per panel
+  case GBPOLY_PREC_FP8 * 8 + 1: return run_fp8<FormFP8_w>(ctx, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
 }

@@ -220,6 +220,8 @@ def test_default_configuration_by_k(ctx):
     assert ctx.config_get(Precision.BF16X3, 8192, 8192, 8192) == 3
     assert ctx.config_get(Precision.TF32, 8192, 8192, 512) == 5
     assert ctx.config_get(Precision.BF16X3, 512, 512, 64) not in (3, 4, 5)
+    assert ctx.config_get(Precision.FP8, 8192, 8192, 8192) == 1  # 128 x 256 tiles
+    assert ctx.config_get(Precision.FP8, 512, 512, 512) == 0
 
 
 @pytest.mark.parametrize("N,ldc", [(90, 96), (300, 304), (256, 260)])

@@ -211,3 +211,34 @@ def test_fp8_syrk_and_syr2k(ctx):
     ctx.synchronize()
     ref2 = oracle.gemm_f64(A, B, C, 1.0, 1.0, op_b=1, A2=B, B2=A)
     assert oracle.error_norms(ctx.download(dC, C.shape), ref2)[1] < 6e-2
+
+
+@pytest.mark.parametrize("op_b", [Op.N, Op.T])
+@pytest.mark.parametrize("mnk", [(256, 512, 512), (200, 300, 300), (384, 256, 128)])
+def test_fp8_wide_tiles_are_bitwise_the_square_ones(ctx, op_b, mnk):
+    """fp8 configuration 1 (128 x 256 tiles) computes every element as
+    configuration 0 (128 x 128): the same scaled chunk sums in the same order;
+    symmetric products set to configuration 1 run configuration 0."""
+    M, N, K = mnk
+    rng = np.random.default_rng(M * N + K)
+    A = _block_scaled(rng, M, K)
+    B = _block_scaled(rng, N, K) if op_b == Op.T else _block_scaled(rng, K, N)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    outs = []
+    for cfg in (0, 1):
+        ctx.config_set(Precision.FP8, M, N, K, cfg)
+        outs.append(run_gemm(ctx, A, B, C, 1.0, 0.25, op_b=op_b, prec=Precision.FP8))
+    ctx.config_set(Precision.FP8, M, N, K, 0)
+    np.testing.assert_array_equal(outs[1].view(np.uint32), outs[0].view(np.uint32))
+    n, k = 300, 200
+    X = rng.standard_normal((n, k)).astype(np.float32)
+    C2 = rng.standard_normal((n, n)).astype(np.float32)
+    dX, dC = ctx.upload(X), ctx.upload(C2)
+    ctx.config_set(Precision.FP8, n, n, k, 1)
+    ctx.syrk(Precision.FP8, n, k, 1.0, dX, k, 1.0, dC, n)
+    ctx.synchronize()
+    ctx.config_set(Precision.FP8, n, n, k, 0)
+    ref = oracle.gemm_f64(X, X, C2, 1.0, 1.0, op_b=1)
+    assert oracle.error_norms(ctx.download(dC, C2.shape), ref)[1] < 6e-2
+    ctx.free(dX)
+    ctx.free(dC)
