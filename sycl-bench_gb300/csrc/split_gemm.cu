@@ -19,14 +19,21 @@
 //       warp 0      TMA producer: the term tiles of A (128 rows) and B (BN rows),
 //                   128-byte rows (64 BF16 or 32 TF32 along K) with 128-byte
 //                   swizzle, into a ring of STAGES shared-memory stages;
-//       warp 1      allocates 2*BN TMEM columns; one lane issues the products'
-//                   tcgen05.mma (M=128, N=BN; K=16 BF16 or K=8 TF32) into one
-//                   of two TMEM chunk buffers, restarting the accumulator
-//                   every CH stages, and commits stages and chunks;
+//       warp 1      allocates all 512 TMEM columns; one lane issues the
+//                   products' tcgen05.mma (M=128, N=BN; K=16 BF16 or K=8 TF32)
+//                   into one of NBUF TMEM chunk buffers (2 of 256 columns or
+//                   4 of 128), restarting the accumulator every CH stages,
+//                   and commits stages and chunks;
 //       warps 4-11  epilogue (setmaxnreg 208): each warp owns 32 rows (its
 //                   TMEM lane quarter) x BN/2 columns and sums the chunks in
 //                   FP32 registers with round-to-nearest adds, then writes
-//                   C = alpha*acc + beta*C.
+//                   C = alpha*acc + beta*C (through a per-warp staging tile,
+//                   or, in the C-tile configurations, through TMA-loaded and
+//                   TMA-stored boxes of C in shared memory).
+//     CTA-pair configurations (cluster of two, cta_group::2) compute 256 x BN
+//     tiles, each CTA staging 128 rows of A and BN/2 rows of B; when a
+//     launch's last round of tiles would leave half the pairs or more idle,
+//     its tiles run as two K halves on two pairs (the K-split tail).
 //     The tensor core accumulates with truncation: over long K its error
 //     grows with the number of MMA steps (measured 3.6e-6 normwise at K=512
 //     for 24-bit operand splits, against 2.6e-7 for the same products summed
