@@ -654,13 +654,18 @@ def run_neighbours(ctx, args) -> dict:
         res = {}
         for prec in (Precision.FP32, Precision.BF16X3, Precision.TF32X3):
             def step(prec=prec):
+                # the drop-in's calls: fp32 centres into a packed copy and contracts it,
+                # the split forms centre inside their split pass (gbpoly_covariance_f32)
                 ctx.column_mean(n, n, X, ld, np.float32(float_n), mu)
+                sd_arg, div = None, np.float32(1.0)
                 if name == "correlation":
                     ctx.column_stddev(n, n, X, ld, mu, np.float32(float_n), np.float32(0.005), sdp)
-                    ctx.center_columns(n, n, X, ld, mu, sdp, np.float32(np.sqrt(float_n)), dY, ldp)
+                    sd_arg, div = sdp, np.float32(np.sqrt(float_n))
+                if prec == Precision.FP32:
+                    ctx.center_columns(n, n, X, ld, mu, sd_arg, div, dY, ldp)
+                    ctx.gemm(prec, n, n, n, 1.0, dY, ldp, dY, ldp, 0.0, S, ld, op_a=Op.T, op_b=Op.N)
                 else:
-                    ctx.center_columns(n, n, X, ld, mu, None, 1.0, dY, ldp)
-                ctx.gemm(prec, n, n, n, 1.0, dY, ldp, dY, ldp, 0.0, S, ld, op_a=Op.T, op_b=Op.N)
+                    ctx.covariance(prec, n, n, X, ld, mu, sd_arg, div, S, ld)
                 if name == "correlation":
                     ctx.set_diagonal(n, 1.0, S, ld)
             step()

@@ -317,6 +317,19 @@ gbpoly_status gbpoly_center_columns_f32(gbpoly_ctx* ctx, int64_t rows, int64_t c
  * and Correlation5 (polybench/correlation.cpp:167-186). */
 gbpoly_status gbpoly_set_diagonal_f32(gbpoly_ctx* ctx, int64_t n, float value, float* C, int64_t ldc);
 
+/* C (cols x cols) = Y^T . Y with Y the centred (stddev == NULL) or centred
+ * and scaled columns of X, as gbpoly_center_columns_f32 defines them: the
+ * covariance / correlation contraction of CovarianceReduce + CovarianceCovar
+ * (polybench/covariance.cpp:98-126) and CorrelationReduce + CorrelationCorr
+ * (polybench/correlation.cpp:144-178) in one call, without a centred copy of
+ * X for the split forms (tf32, bf16x3, tf32x3, bf16x6: the split pass centres
+ * each element before splitting it, with the same arithmetic, so the result
+ * is bitwise that of centring into a copy and contracting it).  fp32 and fp8
+ * centre into a context scratch copy and contract it.  The lower triangle of
+ * tiles is computed and mirrored, so C is the full symmetric square. */
+gbpoly_status gbpoly_covariance_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t rows, int64_t cols, const float* X,
+    int64_t ldx, const float* mean, const float* stddev, float scale_div, float* C, int64_t ldc);
+
 
 /* -------------------------------------------------------------- grouped -- */
 

@@ -204,6 +204,7 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   if(ctx->ws.ptr) cudaFree(ctx->ws.ptr);
   if(ctx->stats.ptr) cudaFree(ctx->stats.ptr);
+  if(ctx->centred.ptr) cudaFree(ctx->centred.ptr);
   for(void* p : {ctx->stage_a, ctx->stage_b, ctx->stage_c})
     if(p) cudaFree(p);
   if(ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);

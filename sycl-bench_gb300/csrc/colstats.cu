@@ -222,6 +222,39 @@ gbpoly_status gbpoly_center_columns_f32(gbpoly_ctx* ctx, int64_t rows, int64_t c
   return GBPOLY_OK;
 }
 
+gbpoly_status gbpoly_covariance_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t rows, int64_t cols, const float* X,
+    int64_t ldx, const float* mean, const float* stddev, float scale_div, float* C, int64_t ldc) {
+  gbpoly_status st = check_args(ctx, rows, cols);
+  if(st != GBPOLY_OK) return st;
+  if((st = check_block("X", X, rows, cols, ldx)) != GBPOLY_OK) return st;
+  if((st = check_block("C", C, cols, cols, ldc)) != GBPOLY_OK) return st;
+  if(cols > 0 && !mean) return fail(GBPOLY_ERR_INVALID, "mean: null pointer");
+  if(cols == 0) return GBPOLY_OK;
+  GemmF32Args a{};
+  a.M = cols, a.N = cols, a.K = rows, a.alpha = 1.f, a.beta = 0.f, a.op_a = GBPOLY_OP_T, a.op_b = GBPOLY_OP_N;
+  a.C = C, a.ldc = ldc;
+  const bool split_form = prec == GBPOLY_PREC_TF32 || prec == GBPOLY_PREC_BF16X3 || prec == GBPOLY_PREC_TF32X3 ||
+                          prec == GBPOLY_PREC_BF16X6;
+  if(split_form && rows > 0) {
+    // centred in the split pass: X itself is both operands
+    a.A = X, a.lda = ldx, a.B = X, a.ldb = ldx;
+    a.xf = RowXform{mean, stddev, scale_div};
+    return launch_gemm_tensor(ctx, prec, a);
+  }
+  if(prec != GBPOLY_PREC_FP32 && prec != GBPOLY_PREC_FP8 && !split_form)
+    return fail(GBPOLY_ERR_INVALID, "unknown precision");
+  // a centred copy with 16-byte-aligned rows, then the contraction
+  const int64_t ldy = (cols + 3) / 4 * 4;
+  if((st = ensure_scratch(ctx, ctx->centred, size_t(std::max<int64_t>(rows, 1)) * size_t(ldy) * 4 + 256,
+          "centred copy")) != GBPOLY_OK)
+    return st;
+  float* Y = static_cast<float*>(ctx->centred.ptr);
+  if((st = gbpoly_center_columns_f32(ctx, rows, cols, X, ldx, mean, stddev, scale_div, Y, ldy)) != GBPOLY_OK)
+    return st;
+  a.A = Y, a.lda = ldy, a.B = Y, a.ldb = ldy;
+  return prec == GBPOLY_PREC_FP32 ? launch_gemm_f32_simt(ctx, a) : launch_gemm_tensor(ctx, prec, a);
+}
+
 gbpoly_status gbpoly_set_diagonal_f32(gbpoly_ctx* ctx, int64_t n, float value, float* C, int64_t ldc) {
   gbpoly_status st = check_args(ctx, n, n);
   if(st != GBPOLY_OK) return st;

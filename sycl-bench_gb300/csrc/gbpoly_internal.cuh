@@ -66,6 +66,7 @@ struct gbpoly_ctx {
   char name[256] = {0};
   gbpoly::Workspace ws;
   gbpoly::Workspace stats;  // per-chunk column partial sums (colstats.cu)
+  gbpoly::Workspace centred;  // gbpoly_covariance_f32, fp32 and fp8 forms: the centred copy of X
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
   bool profiling = false;
   bool tail_split = true;  // K-split units for the last round of CTA-pair tiles
@@ -117,6 +118,17 @@ gbpoly_status make_tmap_2d(gbpoly_ctx* ctx, CUtensorMap* map, CUtensorMapDataTyp
     CUtensorMapSwizzle swizzle);
 
 // FP32 SIMT entry points (sgemm_simt.cu).
+// Per-row transform of op(A) applied by the split pass of the tensor-core
+// forms before splitting (covariance, correlation: op(A) = X^T, a row of
+// op(A) is a column of X): y = x - mean[r], then, with sd, y = (y / div) / sd[r]
+// (the arithmetic of gbpoly_center_columns_f32, so the panels are bitwise
+// those of the centred copy).  mean == nullptr: none.
+struct RowXform {
+  const float* mean = nullptr;
+  const float* sd = nullptr;
+  float div = 1.f;
+};
+
 struct GemmF32Args {
   int64_t M, N, K;
   float alpha, beta;
@@ -137,6 +149,8 @@ struct GemmF32Args {
   // that run a contraction in row panels pass the full shape's split so the
   // panels add K in the same order as the whole call.
   int ksplit = 0;
+  // Tensor-core forms, symmetric products only: transform of op(A)'s rows.
+  RowXform xf;
 };
 // op(B) is op(A)^T on the same stored matrix (syrk's A.A^T, covariance's
 // X^T.X): the product is symmetric, and one set of split panels serves both

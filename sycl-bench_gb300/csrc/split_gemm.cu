@@ -285,7 +285,7 @@ struct SplitTerms<Elem::BF16, TERMS> {
 
 template <Elem E, int TERMS>
 __device__ __forceinline__ void split_convert(const float (*tile)[65], typename Term<E>::T* __restrict__ out,
-    int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0) {
+    int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0, RowXform xf = RowXform{}, int K = 0) {
   using T = typename Term<E>::T;
   const int tid = threadIdx.x;
   const int rr = tid >> 2, kc = (tid & 3) * 16;
@@ -294,6 +294,15 @@ __device__ __forceinline__ void split_convert(const float (*tile)[65], typename 
   float x[16];
 #pragma unroll
   for(int i = 0; i < 16; ++i) x[i] = tile[rr][kc + i];
+  if(xf.mean) {  // the row's transform, on the elements inside K (the K padding stays zero)
+    const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
+#pragma unroll
+    for(int i = 0; i < 16; ++i) {
+      float y = x[i] - m;
+      if(xf.sd) y = (y / xf.div) / sd;
+      x[i] = k0 + kc + i < K ? y : 0.f;
+    }
+  }
   __align__(16) T t[TERMS][16];
   SplitTerms<E, TERMS>::run(x, t);
   constexpr int kVec = 16 * sizeof(T) / 16;  // uint4 per 16 elements
@@ -310,14 +319,14 @@ __device__ __forceinline__ void split_convert(const float (*tile)[65], typename 
 // and `panel_stride` elements apart.  One 64 x 64 block per CTA.
 template <Elem E, int TERMS>
 __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
-    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride) {
+    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride, RowXform xf) {
   __shared__ float tile[64][65];
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
   float v[16];
   const bool whole = split_load(X, ld, k_major, R, K, r0, k0, v);
   split_stage(whole, k_major, v, tile);
   __syncthreads();
-  split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0);
+  split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0, xf, K);
 }
 
 // One operand of a grouped call: its 64x64 blocks are blocks
@@ -1005,12 +1014,12 @@ struct Panels {
 
 template <class F>
 gbpoly_status launch_split(gbpoly_ctx* ctx, const float* X, int64_t ld, bool k_major, int64_t rows, int64_t K,
-    int64_t Kp, Panels out) {
+    int64_t Kp, Panels out, RowXform xf = RowXform{}) {
   using T = typename Term<F::elem>::T;
   dim3 grid(static_cast<unsigned>(Kp / 64), static_cast<unsigned>((rows + 63) / 64));
   ProfileScope prof(ctx, "split_terms");
   split_kernel<F::elem, F::terms><<<grid, 256, 0, ctx->stream>>>(X, ld, k_major ? 1 : 0, int(rows), int(K), int(Kp),
-      reinterpret_cast<T*>(out.base), int64_t(out.stride / sizeof(T)));
+      reinterpret_cast<T*>(out.base), int64_t(out.stride / sizeof(T)), xf);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
 }
@@ -1200,6 +1209,7 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
     return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");
   const bool same = same_operand(a);
+  if(a.xf.mean && !same) return fail(GBPOLY_ERR_UNSUPPORTED, "row transform: symmetric products only");
   const Layout lay = layout<F>(a.M, a.N, a.K, same);
   const int64_t Kp = lay.Kp;
   const size_t a_stride = lay.a_stride, b_stride = lay.b_stride, a_bytes = lay.a_bytes, b_bytes = lay.b_bytes;
@@ -1218,7 +1228,7 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   Panels pa{ws, a_stride};
   Panels pb = same ? pa : Panels{ws + a_bytes, b_stride};
   if(a.K > 0) {
-    if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, Kp, pa)) != GBPOLY_OK) return st;
+    if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, Kp, pa, a.xf)) != GBPOLY_OK) return st;
     if(!same && (st = launch_split<F>(ctx, a.B, a.ldb, a.op_b == GBPOLY_OP_T, a.N, a.K, Kp, pb)) != GBPOLY_OK)
       return st;
   } else {
@@ -1250,6 +1260,7 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
 // FP8 form: quantize both operands (panels + block scales), one MMA product.
 template <class F>
 gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
+  if(a.xf.mean) return fail(GBPOLY_ERR_UNSUPPORTED, "row transform: split forms only");
   if(a.M == 0 || a.N == 0) return GBPOLY_OK;
   if(a.M >= (1ll << 31) || a.N >= (1ll << 31) || a.K >= (1ll << 30))
     return fail(GBPOLY_ERR_UNSUPPORTED, "dimension too large for the tensor-core kernels");

@@ -126,6 +126,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_column_stddev_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_float, ct.c_float, _vp]),
     "gbpoly_center_columns_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, ct.c_float, _vp, _c_i64]),
     "gbpoly_set_diagonal_f32": (ct.c_int, [_vp, _c_i64, ct.c_float, _vp, _c_i64]),
+    "gbpoly_covariance_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, ct.c_float, _vp,
+                                         _c_i64]),
     "gbpoly_grouped_plan": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.POINTER(_vp)]),
     "gbpoly_grouped_run": (ct.c_int, [_vp, _vp]),
     "gbpoly_grouped_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int), ct.POINTER(ct.c_size_t)]),
@@ -445,6 +447,11 @@ class Context:
     def column_stddev(self, rows, cols, X, ldx, mean, divisor, eps, stddev) -> None:
         _check(self.lib.gbpoly_column_stddev_f32(self.handle, rows, cols, _ptr(X), ldx, _ptr(mean), divisor, eps,
                                                  _ptr(stddev)))
+
+    def covariance(self, prec, rows, cols, X, ldx, mean, stddev, scale_div, C, ldc) -> None:
+        """C = Y^T Y, Y the centred (stddev None) or centred and scaled columns of X."""
+        _check(self.lib.gbpoly_covariance_f32(self.handle, int(prec), rows, cols, _ptr(X), ldx, _ptr(mean),
+                                              _ptr(stddev) if stddev is not None else None, scale_div, _ptr(C), ldc))
 
     def center_columns(self, rows, cols, X, ldx, mean, stddev, scale_div, Y, ldy) -> None:
         _check(self.lib.gbpoly_center_columns_f32(self.handle, rows, cols, _ptr(X), ldx, _ptr(mean),

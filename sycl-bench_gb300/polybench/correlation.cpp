@@ -15,6 +15,9 @@
 // The reference divides by the double constants FLOAT_N and sqrt(FLOAT_N) in
 // CorrelationStd and CorrelationReduce; the device passes use their float
 // roundings (each quotient moves by at most one unit in the last place).
+// With a split precision form, CorrelationReduce launches nothing and
+// CorrelationCorr is gbpoly_covariance_f32, whose split pass centres and
+// scales each element as it splits it (same bits, one pass fewer).
 #include <cmath>
 #include <string>
 #include <vector>
@@ -104,9 +107,11 @@ public:
       gb::check(gbpoly_column_stddev_f32(h.ctx(), n, n, X, int64_t(ld), mu, float(FLOAT_N), float(EPS), sd),
           "column stddev");
     }));
+    const bool fused = poly::centres_in_split(opt.precision);
     // CorrelationReduce
     events.push_back(args.device_queue.submit([&](gb::Handler& h) {
       if(h.on_host()) return host_reduce(X, mu, sd);
+      if(fused) return;  // centred and scaled in the contraction's split pass
       gb::check(gbpoly_center_columns_f32(h.ctx(), n, n, X, int64_t(ld), mu, sd, float(std::sqrt(FLOAT_N)),
                     centered_buffer.get(), int64_t(ldp)),
           "normalize columns");
@@ -114,6 +119,10 @@ public:
     // CorrelationCorr
     events.push_back(args.device_queue.submit([&](gb::Handler& h) {
       if(h.on_host()) return host_corr(X, S);
+      if(fused)
+        return gb::check(gbpoly_covariance_f32(h.ctx(), opt.precision, n, n, X, int64_t(ld), mu, sd,
+                             float(std::sqrt(FLOAT_N)), S, int64_t(ld)),
+            "correlation contraction");
       const float* Y = centered_buffer.get();
       gb::check(gbpoly_gemm_f32(h.ctx(), opt.precision, GBPOLY_OP_T, GBPOLY_OP_N, n, n, n, 1.f, Y, int64_t(ldp), Y,
                     int64_t(ldp), 0.f, S, int64_t(ld)),

@@ -10,6 +10,9 @@
 //   CovarianceCovar  (covariance.cpp:108-126) gbpoly_gemm_f32(op_a = T,
 //       op_b = N, A == B): the symmetric contraction, lower triangle of tiles
 //       computed and mirrored; the reference computes j2 >= j1 and mirrors.
+// With a split precision form, CovarianceReduce launches nothing and
+// CovarianceCovar is gbpoly_covariance_f32, whose split pass centres each
+// element as it splits it (same bits, one pass over the data fewer).
 #include <cmath>
 #include <string>
 #include <vector>
@@ -74,9 +77,11 @@ public:
       if(h.on_host()) return host_mean(X, mu);
       gb::check(gbpoly_column_mean_f32(h.ctx(), n, n, X, int64_t(ld), float_n, mu), "column mean");
     }));
+    const bool fused = poly::centres_in_split(opt.precision);
     // CovarianceReduce
     events.push_back(args.device_queue.submit([&](gb::Handler& h) {
       if(h.on_host()) return host_center(X, mu);
+      if(fused) return;  // centred in the contraction's split pass
       gb::check(gbpoly_center_columns_f32(h.ctx(), n, n, X, int64_t(ld), mu, nullptr, 1.f, centered_buffer.get(),
                     int64_t(ldp)),
           "center columns");
@@ -84,6 +89,10 @@ public:
     // CovarianceCovar
     events.push_back(args.device_queue.submit([&](gb::Handler& h) {
       if(h.on_host()) return host_covar(X, S);
+      if(fused)
+        return gb::check(gbpoly_covariance_f32(h.ctx(), opt.precision, n, n, X, int64_t(ld), mu, nullptr, 1.f, S,
+                             int64_t(ld)),
+            "covariance contraction");
       const float* Y = centered_buffer.get();
       gb::check(gbpoly_gemm_f32(h.ctx(), opt.precision, GBPOLY_OP_T, GBPOLY_OP_N, n, n, n, 1.f, Y, int64_t(ldp), Y,
                     int64_t(ldp), 0.f, S, int64_t(ld)),

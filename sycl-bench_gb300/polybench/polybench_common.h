@@ -95,6 +95,12 @@ inline std::vector<gbpoly_precision> precisions(const BenchmarkArgs& args) {
 
 // The matrix-vector benchmarks run the plain FP32 form only (HBM-bound, no
 // contraction for the tensor cores): --precision may name fp32 alone.
+// Precision forms whose split pass can centre (and scale) the columns of the
+// covariance / correlation data itself (gbpoly_covariance_f32).
+inline bool centres_in_split(gbpoly_precision p) {
+  return p == GBPOLY_PREC_TF32 || p == GBPOLY_PREC_BF16X3 || p == GBPOLY_PREC_TF32X3 || p == GBPOLY_PREC_BF16X6;
+}
+
 inline void require_fp32_only(const BenchmarkArgs& args) {
   for(auto p : precisions(args))
     if(p != GBPOLY_PREC_FP32)

@@ -198,3 +198,31 @@ def test_fp32_syr2k_triangle_against_fp64(ctx):
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-6
     for x in (dA, dB, dC):
         ctx.free(x)
+
+
+@pytest.mark.parametrize("prec", FORMS + [Precision.TF32, Precision.FP8], ids=lambda p: p.name.lower())
+@pytest.mark.parametrize("n", [100, 257, 640])
+@pytest.mark.parametrize("scaled", [False, True], ids=["covariance", "correlation"])
+def test_covariance_call_is_bitwise_the_chain(ctx, prec, n, scaled):
+    # gbpoly_covariance_f32 (the split forms centre inside their split pass)
+    # gives the bits of centring into a copy and contracting the copy
+    ld, ldp = n + 1, ldp_of(n)
+    data = oracle.init_correlation(n) if scaled else oracle.init_covariance(n)
+    d = ctx.upload(data)
+    mean, sd = ctx.upload(np.zeros(ld, np.float32)), ctx.upload(np.zeros(ld, np.float32))
+    S1, S2 = ctx.upload(np.zeros((ld, ld), np.float32)), ctx.upload(np.zeros((ld, ld), np.float32))
+    Y = ctx.alloc(max(n * ldp, 1) * 4)
+    X, mu, sdp = d.ptr + (ld + 1) * 4, mean.ptr + 4, sd.ptr + 4
+    fn = np.float32(CORR_FLOAT_N) if scaled else COV_FLOAT_N
+    ctx.column_mean(n, n, X, ld, fn, mu)
+    if scaled:
+        ctx.column_stddev(n, n, X, ld, mu, fn, np.float32(CORR_EPS), sdp)
+    div = np.float32(np.sqrt(CORR_FLOAT_N)) if scaled else np.float32(1.0)
+    ctx.center_columns(n, n, X, ld, mu, sdp if scaled else None, div, Y, ldp)
+    ctx.gemm(prec, n, n, n, 1.0, Y, ldp, Y, ldp, 0.0, S1.ptr + (ld + 1) * 4, ld, op_a=Op.T, op_b=Op.N)
+    ctx.covariance(prec, n, n, X, ld, mu, sdp if scaled else None, div, S2.ptr + (ld + 1) * 4, ld)
+    ctx.synchronize()
+    a, b = ctx.download(S1, (ld, ld)), ctx.download(S2, (ld, ld))
+    np.testing.assert_array_equal(b.view(np.uint32), a.view(np.uint32))
+    for buf in (d, mean, sd, S1, S2, Y):
+        ctx.free(buf)
