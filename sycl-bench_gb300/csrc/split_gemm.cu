@@ -1527,6 +1527,7 @@ struct gbpoly_grouped {
   int* block_job = nullptr;  // split block -> job
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
+  bool pairs = false;  // CTA-pair (256 x 256) tiles instead of 128 x 128
 };
 
 namespace gbpoly {
@@ -1632,11 +1633,32 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
   return launch_tc_kernel<F>(ctx, sched, g->ntiles, name);
 }
 
-// Grouped calls use the 128-column tile configurations (less padding on small problems).
+// Grouped calls use the 128-column tile configurations (less padding on
+// small problems), or the CTA-pair configurations when every problem is
+// large enough that 256 x 256 tiles pad it about as little and the group
+// fills at least two rounds of pairs (a few large products, as matmulchain's
+// two independent stages).
 using GroupBF16x3 = FormBF16x3_c;
 using GroupTF32x3 = FormTF32x3_c;
 using GroupBF16x6 = FormBF16x6_b;
 using GroupTF32 = FormTF32_c;
+using GroupBF16x3_p = FormBF16x3_p;
+using GroupTF32x3_p = FormTF32x3_p;
+using GroupBF16x6_p = FormBF16x6_p;
+using GroupTF32_p = FormTF32_p;
+
+bool grouped_pairs(gbpoly_ctx* ctx, const std::vector<gbpoly_gemm_desc>& descs) {
+  double work128 = 0, work256 = 0;
+  int64_t pair_tiles = 0;
+  for(const auto& d : descs) {
+    if(d.M <= 0 || d.N <= 0) continue;
+    const double k = double(std::max<int64_t>(d.K, 1));
+    work128 += double((d.M + 127) / 128 * 128) * double((d.N + 127) / 128 * 128) * k;
+    work256 += double((d.M + 255) / 256 * 256) * double((d.N + 255) / 256 * 256) * k;
+    pair_tiles += ((d.M + 255) / 256) * ((d.N + 255) / 256);
+  }
+  return pair_tiles >= ctx->sm_count && work256 <= 1.05 * work128;
+}
 
 }  // namespace
 }  // namespace gbpoly
@@ -1678,10 +1700,22 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
     if(ws > 0) st = ensure_workspace(ctx, ws);
     break;
   }
-  case GBPOLY_PREC_BF16X3: st = plan_grouped<GroupBF16x3>(ctx, g); break;
-  case GBPOLY_PREC_TF32X3: st = plan_grouped<GroupTF32x3>(ctx, g); break;
-  case GBPOLY_PREC_BF16X6: st = plan_grouped<GroupBF16x6>(ctx, g); break;
-  case GBPOLY_PREC_TF32: st = plan_grouped<GroupTF32>(ctx, g); break;
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_TF32X3:
+  case GBPOLY_PREC_BF16X6:
+  case GBPOLY_PREC_TF32:
+    g->pairs = grouped_pairs(ctx, g->descs);
+    switch(prec * 2 + (g->pairs ? 1 : 0)) {
+    case GBPOLY_PREC_BF16X3 * 2: st = plan_grouped<GroupBF16x3>(ctx, g); break;
+    case GBPOLY_PREC_BF16X3 * 2 + 1: st = plan_grouped<GroupBF16x3_p>(ctx, g); break;
+    case GBPOLY_PREC_TF32X3 * 2: st = plan_grouped<GroupTF32x3>(ctx, g); break;
+    case GBPOLY_PREC_TF32X3 * 2 + 1: st = plan_grouped<GroupTF32x3_p>(ctx, g); break;
+    case GBPOLY_PREC_BF16X6 * 2: st = plan_grouped<GroupBF16x6>(ctx, g); break;
+    case GBPOLY_PREC_BF16X6 * 2 + 1: st = plan_grouped<GroupBF16x6_p>(ctx, g); break;
+    case GBPOLY_PREC_TF32 * 2: st = plan_grouped<GroupTF32>(ctx, g); break;
+    default: st = plan_grouped<GroupTF32_p>(ctx, g); break;
+    }
+    break;
   default: st = fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   }
   if(st != GBPOLY_OK) {
@@ -1707,10 +1741,18 @@ gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
       if(st != GBPOLY_OK) return st;
     }
     return GBPOLY_OK;
-  case GBPOLY_PREC_BF16X3: return run_grouped<GroupBF16x3>(ctx, g, "grouped_bf16x3_gemm");
-  case GBPOLY_PREC_TF32X3: return run_grouped<GroupTF32x3>(ctx, g, "grouped_tf32x3_gemm");
-  case GBPOLY_PREC_BF16X6: return run_grouped<GroupBF16x6>(ctx, g, "grouped_bf16x6_gemm");
-  case GBPOLY_PREC_TF32: return run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
+  case GBPOLY_PREC_BF16X3:
+    return g->pairs ? run_grouped<GroupBF16x3_p>(ctx, g, "grouped_bf16x3_gemm")
+                    : run_grouped<GroupBF16x3>(ctx, g, "grouped_bf16x3_gemm");
+  case GBPOLY_PREC_TF32X3:
+    return g->pairs ? run_grouped<GroupTF32x3_p>(ctx, g, "grouped_tf32x3_gemm")
+                    : run_grouped<GroupTF32x3>(ctx, g, "grouped_tf32x3_gemm");
+  case GBPOLY_PREC_BF16X6:
+    return g->pairs ? run_grouped<GroupBF16x6_p>(ctx, g, "grouped_bf16x6_gemm")
+                    : run_grouped<GroupBF16x6>(ctx, g, "grouped_bf16x6_gemm");
+  case GBPOLY_PREC_TF32:
+    return g->pairs ? run_grouped<GroupTF32_p>(ctx, g, "grouped_tf32_gemm")
+                    : run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   }
 }

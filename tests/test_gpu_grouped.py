@@ -99,3 +99,38 @@ def test_grouped_rejects_bad_descriptor(ctx):
     with pytest.raises(gbpoly.GbpolyError) as e:
         ctx.grouped_plan(Precision.BF16X3, descs)
     assert e.value.status == gbpoly.Status.INVALID and b"problem 0" in ctx.lib.gbpoly_last_error()
+
+
+@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.TF32X3])
+def test_grouped_large_problems_run_on_cta_pairs(ctx, prec):
+    # a few large products (256 x 256 tiles pad them no more than 128 x 128
+    # ones, and they fill two rounds of pairs) run on CTA-pair tiles: each
+    # result is bitwise the single-call result of the pair configuration
+    rng = np.random.default_rng(31)
+    probs = []
+    for i, (M, N, K) in enumerate([(2048, 2048, 512), (2048, 1792, 384), (1536, 2048, 640)]):
+        op_b = Op.T if i == 1 else Op.N
+        A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+        B = rng.uniform(-1, 1, (N, K) if op_b == Op.T else (K, N)).astype(np.float32)
+        C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+        probs.append((Op.N, op_b, M, N, K, A, B, C))
+    plan, bufs = run_group(ctx, prec, probs)
+    ctx.grouped_run(plan)
+    ctx.synchronize()
+    for (op_a, op_b, M, N, K, A, B, C), (_, _, dC) in zip(probs, bufs):
+        got = ctx.download(dC, (M, N))
+        dA, dB, dS = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+        ctx.config_set(prec, M, N, K, 3)
+        ctx.tail_split(False)
+        ctx.gemm(prec, M, N, K, 1.0, dA, K, dB, B.shape[1], 0.5, dS, N, op_a=op_a, op_b=op_b)
+        ctx.synchronize()
+        ctx.tail_split(True)
+        ctx.config_set(prec, M, N, K, 0)
+        single = ctx.download(dS, (M, N))
+        np.testing.assert_array_equal(got.view(np.uint32), single.view(np.uint32))
+        for b in (dA, dB, dS):
+            ctx.free(b)
+    ctx.grouped_destroy(plan)
+    for b in bufs:
+        for x in b:
+            ctx.free(x)
