@@ -3,6 +3,9 @@
 // verification loop and CSV columns; each stage is a libgbpoly contraction.
 // The reference accumulates each stage onto zero-initialised E, F, G; the
 // stages here write their output (beta = 0), which is the same value.
+// Options beyond the reference's: --graph (the stages as one captured CUDA
+// graph) and --grouped (E and F, which are independent, as one grouped
+// launch; the float benchmark only).
 #include <string>
 #include <vector>
 
@@ -52,10 +55,13 @@ class Polybench_3mm {
 public:
   Polybench_3mm(const BenchmarkArgs& args, gbpoly_precision prec = GBPOLY_PREC_FP32)
       : args(args), size(args.problem_size), opt(poly::options(args, prec)),
-        use_graph(args.cli.isFlagSet("--graph") && !args.device_queue.is_host()) {}
+        use_graph(args.cli.isFlagSet("--graph") && !args.device_queue.is_host()),
+        use_grouped(std::is_same<T, float>::value && args.cli.isFlagSet("--grouped") &&
+                    !args.device_queue.is_host()) {}
 
   ~Polybench_3mm() {
     if(graph) gbpoly_graph_destroy(args.device_queue.ctx(), graph);
+    if(grouped) gbpoly_grouped_destroy(args.device_queue.ctx(), grouped);
   }
 
   void setup() {
@@ -69,6 +75,7 @@ public:
     E_buffer.initialize(args.device_queue, E.data(), nn);
     F_buffer.initialize(args.device_queue, F.data(), nn);
     G_buffer.initialize(args.device_queue, G.data(), nn);
+    if(use_grouped) plan_grouped();
     if(use_graph) capture_stages();
   }
 
@@ -78,8 +85,13 @@ public:
           [&](gb::Handler& h) { gb::check(gbpoly_graph_launch(h.ctx(), graph), "graph launch"); }));
       return;
     }
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 0); }));  // E = A.B (3mm.cpp:120-127)
-    events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 1); }));  // F = C.D (3mm.cpp:135-142)
+    if(use_grouped) {  // E and F, which are independent, as one grouped launch
+      events.push_back(args.device_queue.submit(
+          [&](gb::Handler& h) { gb::check(gbpoly_grouped_run(h.ctx(), grouped), "grouped run"); }));
+    } else {
+      events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 0); }));  // E = A.B (3mm.cpp:120-127)
+      events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 1); }));  // F = C.D (3mm.cpp:135-142)
+    }
     events.push_back(args.device_queue.submit([&](gb::Handler& h) { stage(h, 2); }));  // G = E.F (3mm.cpp:150-157)
   }
 
@@ -107,7 +119,7 @@ public:
   }
 
   std::string getBenchmarkName(const BenchmarkArgs&) const {
-    return poly::variant_name<T>("Polybench_3mm", opt) + (use_graph ? "_graph" : "");
+    return poly::variant_name<T>("Polybench_3mm", opt) + (use_grouped ? "_grouped" : "") + (use_graph ? "_graph" : "");
   }
 
   static ThroughputMetric getThroughputMetric(const BenchmarkArgs& args) {
@@ -133,8 +145,32 @@ private:
     }
     gb::Handler h(args.device_queue);
     gb::check(gbpoly_graph_begin(ctx), "graph begin");
-    for(int i = 0; i < 3; ++i) stage(h, i);
+    if(use_grouped)
+      gb::check(gbpoly_grouped_run(ctx, grouped), "grouped run");
+    else
+      for(int i = 0; i < 2; ++i) stage(h, i);
+    stage(h, 2);
     gb::check(gbpoly_graph_end(ctx, &graph), "graph end");
+  }
+
+  // --grouped: E = A.B and F = C.D as one plan (untimed, in setup)
+  void plan_grouped() {
+    if constexpr(std::is_same<T, float>::value) {
+      const int64_t n = int64_t(size);
+      gbpoly_gemm_desc d[2] = {};
+      const T* ops[2][2] = {{A_buffer.get(), B_buffer.get()}, {C_buffer.get(), D_buffer.get()}};
+      T* outs[2] = {E_buffer.get(), F_buffer.get()};
+      for(int i = 0; i < 2; ++i) {
+        d[i].op_a = d[i].op_b = GBPOLY_OP_N;
+        d[i].M = d[i].N = d[i].K = n;
+        d[i].alpha = 1.f;
+        d[i].beta = 0.f;
+        d[i].A = ops[i][0], d[i].lda = n;
+        d[i].B = ops[i][1], d[i].ldb = n;
+        d[i].C = outs[i], d[i].ldc = n;
+      }
+      gb::check(gbpoly_grouped_plan(args.device_queue.ctx(), opt.precision, d, 2, &grouped), "grouped plan");
+    }
   }
 
   void contract(gb::Handler& h, const T* a, const T* b, T* out) {
@@ -184,8 +220,9 @@ private:
   BenchmarkArgs args;
   const size_t size;
   poly::Options opt;
-  bool use_graph;
+  bool use_graph, use_grouped;
   gbpoly_graph* graph = nullptr;
+  gbpoly_grouped* grouped = nullptr;
   std::vector<T> A, B, C, D, E, F, G;
   PrefetchedBuffer<T, 2> A_buffer, B_buffer, C_buffer, D_buffer, E_buffer, F_buffer, G_buffer;
 };

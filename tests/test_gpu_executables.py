@@ -70,6 +70,18 @@ def test_graph_mode_verifies(bench):
     assert out.count("Verification: PASS") == 3, out
 
 
+@pytest.mark.parametrize("flags", [("--grouped",), ("--grouped", "--graph")])
+def test_3mm_grouped_mode_verifies(flags):
+    # E and F as one grouped launch (with or without the graph); the double
+    # variant keeps its three launches
+    out = run("3mm", "--size=300", "--num-runs=2", *flags, "--precision=fp32,bf16x3")
+    base = BENCHES["3mm"]
+    names = re.findall(r"Results for (\S+?)\*", out)
+    sfx = "_grouped" + ("_graph" if "--graph" in flags else "")
+    assert names == [base + sfx, base + "_bf16x3" + sfx, base + "_fp64" + ("_graph" if "--graph" in flags else "")]
+    assert out.count("Verification: PASS") == 3, out
+
+
 @pytest.mark.parametrize("size", [257, 1024])
 @pytest.mark.parametrize("bench", list(FLOAT_ONLY))
 def test_float_only_benchmarks_verify_on_gpu(bench, size):
