@@ -78,3 +78,22 @@ def test_workspace_query_is_host_logic():
     assert small > 0 and small % (1024 * 1024 * 4) == 0
     assert query(Precision.FP32, 1024, 1024, 16) == 0  # too little K to split
     assert lib.gbpoly_workspace_query(int(Precision.FP32), -1, 4, 4, 0, ct.byref(ct.c_size_t())) != 0
+
+
+def test_null_context_is_an_error_not_a_crash():
+    # entry points check their context before any CUDA call: on a machine
+    # without a GPU they return GBPOLY_ERR_INVALID with a message
+    import ctypes as ct
+
+    import gbpoly
+    from gbpoly import Precision
+
+    if not gbpoly.LIB_PATH.exists():
+        pytest.skip("libgbpoly.so not built")
+    lib = gbpoly.load_library()
+    invalid = 1  # GBPOLY_ERR_INVALID
+    assert lib.gbpoly_covariance_f32(None, int(Precision.BF16X3), 4, 4, None, 4, None, None, 1.0, None, 4) == invalid
+    assert b"context" in lib.gbpoly_last_error()
+    assert lib.gbpoly_center_columns_f32(None, 4, 4, None, 4, None, None, 1.0, None, 4) == invalid
+    assert lib.gbpoly_tail_split_enable(None, 1) == invalid
+    assert lib.gbpoly_profile_enable(None, 1) == invalid
