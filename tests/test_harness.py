@@ -74,6 +74,17 @@ def test_statistics_benchmarks_seeded_and_error_report(bench, tmp_path):
     assert len(rows) == 1 and rows[0]["init"] == "uniform" and rows[0]["frob_rel"] < 1e-5
 
 
+def test_error_report_one_line_per_configuration(tmp_path):
+    # verify() runs after every run; the report keeps one line per benchmark
+    # configuration, and the double variant is labelled fp64
+    rep = tmp_path / "g.jsonl"
+    run("gemm", "--size=48", "--device=cpu", "--num-runs=3", "--init=uniform", f"--error-report={rep}")
+    rows = [json.loads(x) for x in rep.read_text().splitlines()]
+    assert [(r["benchmark"], r["precision"]) for r in rows] == [
+        ("Polybench_Gemm_uniform_seed1", "fp32"), ("Polybench_Gemm_fp64_uniform_seed1", "fp64")]
+    assert rows[1]["frob_rel"] < 1e-13
+
+
 @pytest.mark.parametrize("bench", ["atax", "bicg", "mvt", "gesummv"])
 def test_matrix_vector_benchmarks_fp32_only_and_error_report(bench, tmp_path):
     assert "fp32 form only" in run(bench, "--size=16", "--device=cpu", "--precision=bf16x3").stderr
@@ -143,7 +154,7 @@ def test_error_report_and_variants(tmp_path):
               f"--error-report={rep}").stdout
     assert "Results for Polybench_Syr2k_normal_seed7" in out
     lines = [json.loads(x) for x in rep.read_text().splitlines()]
-    assert len(lines) == 4  # two runs x (fp32, fp64)
+    assert len(lines) == 2  # one line per configuration (fp32, fp64), not per run
     assert all(x["init"] == "normal" and x["seed"] == 7 for x in lines)
     fp32 = [x for x in lines if x["benchmark"] == "Polybench_Syr2k_normal_seed7"]
     assert fp32 and all(x["frob_rel"] < 1e-5 for x in fp32)
