@@ -218,15 +218,8 @@ private:
       }
   }
   void host_corr(const float* X, float* S) const {
-#pragma omp parallel for schedule(dynamic, 4)
-    for(long j1 = 0; j1 < long(size); ++j1) {
-      S[j1 * ld + j1] = 1.0;
-      for(size_t j2 = j1 + 1; j2 < size; j2++) {
-        S[j1 * ld + j2] = 0.0;
-        for(size_t i = 0; i < size; i++) S[j1 * ld + j2] += X[i * ld + j1] * X[i * ld + j2];
-        S[j2 * ld + j1] = S[j1 * ld + j2];
-      }
-    }
+    for(size_t j = 0; j < size; j++) S[j * ld + j] = 1.0;
+    poly::host_xtx_upper(size, ld, X, S, 1);
   }
 
   // FP64 result of the same program: statistics, standardisation and the

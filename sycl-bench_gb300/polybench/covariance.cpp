@@ -167,17 +167,8 @@ private:
     for(long i = 0; i < long(size); ++i)
       for(size_t j = 0; j < size; ++j) X[i * ld + j] -= mu[j];
   }
-  void host_covar(const float* X, float* S) const {
-#pragma omp parallel for schedule(dynamic, 4)
-    for(long j1 = 0; j1 < long(size); ++j1) {
-      S[j1 * ld + j1] = 1.0;
-      for(size_t j2 = j1; j2 < size; j2++) {
-        S[j1 * ld + j2] = 0.0;
-        for(size_t i = 0; i < size; i++) S[j1 * ld + j2] += X[i * ld + j1] * X[i * ld + j2];
-        S[j2 * ld + j1] = S[j1 * ld + j2];
-      }
-    }
-  }
+  // The diagonal's 1.0 (covariance.cpp:118) is overwritten by its own sum.
+  void host_covar(const float* X, float* S) const { poly::host_xtx_upper(size, ld, X, S, 0); }
 
   // FP64 result of the same program: means, centring and the contraction in
   // double (the divisor is the float constant the program uses).

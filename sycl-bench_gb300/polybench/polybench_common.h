@@ -364,4 +364,32 @@ void host_gemm_body(std::size_t n, bool tb, T alpha, const T* A, const T* B, T b
   }
 }
 
+// S[j1][j2] = S[j2][j1] = sum_i X[i][j1] * X[i][j2] over n x n X (leading
+// dimension ld) for j2 >= j1 + skip, each sum from 0 with i in order: the
+// XᵀX kernels of covariance.cpp:114-126 (skip 0) and correlation.cpp:167-181
+// (skip 1; the unit diagonal is the caller's).  OpenMP over j1, a 64-wide
+// block of j2 vectorised over contiguous row segments; the same operations
+// on every element as the per-element loop.
+template <class T>
+void host_xtx_upper(std::size_t n, std::size_t ld, const T* X, T* S, std::size_t skip) {
+  constexpr std::size_t V = 64;
+#pragma omp parallel for schedule(dynamic, 4)
+  for(long j1 = 0; j1 < long(n); ++j1) {
+    for(std::size_t b0 = std::size_t(j1) + skip; b0 < n; b0 += V) {
+      const std::size_t b1 = std::min(n, b0 + V);
+      T acc[V];
+      for(std::size_t j = b0; j < b1; ++j) acc[j - b0] = T(0);
+      for(std::size_t i = 0; i < n; ++i) {
+        const T x = X[i * ld + std::size_t(j1)];
+        const T* row = X + i * ld;
+        for(std::size_t j = b0; j < b1; ++j) acc[j - b0] += x * row[j];
+      }
+      for(std::size_t j = b0; j < b1; ++j) {
+        S[std::size_t(j1) * ld + j] = acc[j - b0];
+        S[j * ld + std::size_t(j1)] = acc[j - b0];
+      }
+    }
+  }
+}
+
 }  // namespace poly
