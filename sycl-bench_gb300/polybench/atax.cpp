@@ -121,25 +121,7 @@ private:
     for(long i = 0; i < long(size); ++i)
       for(size_t j = 0; j < size; j++) t[i] += a[i * size + j] * xv[j];
   }
-  // y[j] += A[i][j] * tmp[i] with i in order for each j; a thread owns a
-  // block of 64 columns and walks the rows, so each row segment is one
-  // contiguous read instead of one cache line per element.
-  void host_cols(const float* a, const float* t, float* yv) const {
-    constexpr size_t V = 64;
-    const long blocks = long((size + V - 1) / V);
-#pragma omp parallel for schedule(static)
-    for(long b = 0; b < blocks; ++b) {
-      const size_t j0 = size_t(b) * V, j1 = std::min(size, j0 + V);
-      float acc[V];
-      for(size_t j = j0; j < j1; j++) acc[j - j0] = yv[j];
-      for(size_t i = 0; i < size; i++) {
-        const float ti = t[i];
-        const float* row = a + i * size;
-        for(size_t j = j0; j < j1; j++) acc[j - j0] += row[j] * ti;
-      }
-      for(size_t j = j0; j < j1; j++) yv[j] = acc[j - j0];
-    }
-  }
+  void host_cols(const float* a, const float* t, float* yv) const { poly::host_gemv_t_body(size, a, t, yv); }
 
   BenchmarkArgs args;
   const size_t size;

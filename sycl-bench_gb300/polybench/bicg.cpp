@@ -128,24 +128,7 @@ private:
   }
 
   // --device=cpu: the reference kernel bodies (bicg.cpp:82-98) on the host cores
-  // s[j] += A[i][j] * r[i] with i in order for each j; a thread owns a block
-  // of 64 columns and walks the rows (contiguous row segments).
-  void host_cols(const float* a, const float* rv, float* sv) const {
-    constexpr size_t V = 64;
-    const long blocks = long((size + V - 1) / V);
-#pragma omp parallel for schedule(static)
-    for(long b = 0; b < blocks; ++b) {
-      const size_t j0 = size_t(b) * V, j1 = std::min(size, j0 + V);
-      float acc[V];
-      for(size_t j = j0; j < j1; j++) acc[j - j0] = sv[j];
-      for(size_t i = 0; i < size; i++) {
-        const float ri = rv[i];
-        const float* row = a + i * size;
-        for(size_t j = j0; j < j1; j++) acc[j - j0] += row[j] * ri;
-      }
-      for(size_t j = j0; j < j1; j++) sv[j] = acc[j - j0];
-    }
-  }
+  void host_cols(const float* a, const float* rv, float* sv) const { poly::host_gemv_t_body(size, a, rv, sv); }
   void host_rows(const float* a, const float* pv, float* qv) const {
 #pragma omp parallel for schedule(static)
     for(long i = 0; i < long(size); ++i)

@@ -364,6 +364,50 @@ void host_gemm_body(std::size_t n, bool tb, T alpha, const T* A, const T* B, T b
   }
 }
 
+// C[i][j] = beta*C[i][j] + sum_k (alpha*A[i][k]*B[j][k] + alpha*B[i][k]*A[j][k])
+// with k in order and one statement per k (syr2k.cpp:78-87).  A and B are
+// transposed once so that a 64-wide block of j reads contiguous rows of Aᵀ
+// and Bᵀ; the operations per element are those of the per-element loop.
+template <class T>
+void host_syr2k_body(std::size_t n, T alpha, const T* A, const T* B, T beta, T* C) {
+  const std::vector<T> at = host_transpose(n, A), bt = host_transpose(n, B);
+  constexpr std::size_t V = 64;
+#pragma omp parallel for schedule(static)
+  for(long i = 0; i < long(n); i++)
+    for(std::size_t j0 = 0; j0 < n; j0 += V) {
+      const std::size_t j1 = std::min(n, j0 + V);
+      T c[V];
+      for(std::size_t j = j0; j < j1; j++) c[j - j0] = C[i * n + j] * beta;
+      for(std::size_t k = 0; k < n; k++) {
+        const T a = alpha * A[i * n + k], b = alpha * B[i * n + k];
+        const T *bk = bt.data() + k * n, *ak = at.data() + k * n;
+        for(std::size_t j = j0; j < j1; j++) c[j - j0] += a * bk[j] + b * ak[j];
+      }
+      for(std::size_t j = j0; j < j1; j++) C[i * n + j] = c[j - j0];
+    }
+}
+
+// y[j] += A[i][j] * x[i] for an n x n row-major A, i in order for each j: the
+// transposed matrix-vector kernels (atax.cpp:87-95, bicg.cpp:77-84).  A thread
+// owns a block of 64 columns and walks the rows, so each row segment is one
+// contiguous read instead of one cache line per element.
+inline void host_gemv_t_body(std::size_t n, const float* A, const float* x, float* y) {
+  constexpr std::size_t V = 64;
+  const long blocks = long((n + V - 1) / V);
+#pragma omp parallel for schedule(static)
+  for(long b = 0; b < blocks; ++b) {
+    const std::size_t j0 = std::size_t(b) * V, j1 = std::min(n, j0 + V);
+    float acc[V];
+    for(std::size_t j = j0; j < j1; j++) acc[j - j0] = y[j];
+    for(std::size_t i = 0; i < n; i++) {
+      const float xi = x[i];
+      const float* row = A + i * n;
+      for(std::size_t j = j0; j < j1; j++) acc[j - j0] += row[j] * xi;
+    }
+    for(std::size_t j = j0; j < j1; j++) y[j] = acc[j - j0];
+  }
+}
+
 // S[j1][j2] = S[j2][j1] = sum_i X[i][j1] * X[i][j2] over n x n X (leading
 // dimension ld) for j2 >= j1 + skip, each sum from 0 with i in order: the
 // XᵀX kernels of covariance.cpp:114-126 (skip 0) and correlation.cpp:167-181

@@ -36,29 +36,6 @@ void syr2k(const T* A, const T* B, T* C, size_t size, T alpha, T beta) {
       }
 }
 
-// Device kernel body on the host cores (syr2k.cpp:78-87, one statement per k):
-// c += alpha*A[i][k]*B[j][k] + alpha*B[i][k]*A[j][k] with k in order for each
-// element.  A and B are transposed once so that a 64-wide block of j reads
-// contiguous rows of A^T and B^T; the operations per element are unchanged.
-template <class T>
-void syr2k_body(const T* A, const T* B, T* C, size_t n, T alpha, T beta) {
-  const std::vector<T> at = poly::host_transpose(n, A), bt = poly::host_transpose(n, B);
-  constexpr size_t V = 64;
-#pragma omp parallel for schedule(static)
-  for(long i = 0; i < long(n); i++)
-    for(size_t j0 = 0; j0 < n; j0 += V) {
-      const size_t j1 = std::min(n, j0 + V);
-      T c[V];
-      for(size_t j = j0; j < j1; j++) c[j - j0] = C[i * n + j] * beta;
-      for(size_t k = 0; k < n; k++) {
-        const T a = alpha * A[i * n + k], b = alpha * B[i * n + k];
-        const T *bk = bt.data() + k * n, *ak = at.data() + k * n;
-        for(size_t j = j0; j < j1; j++) c[j - j0] += a * bk[j] + b * ak[j];
-      }
-      for(size_t j = j0; j < j1; j++) C[i * n + j] = c[j - j0];
-    }
-}
-
 template <class T>
 class Polybench_Syr2k {
 public:
@@ -81,7 +58,7 @@ public:
   void run(std::vector<gb::Event>& events) {
     events.push_back(args.device_queue.submit([&](gb::Handler& h) {
       if(h.on_host()) {
-        syr2k_body<T>(A_buffer.get(), B_buffer.get(), C_buffer.get(), size, alpha, beta);
+        poly::host_syr2k_body<T>(size, alpha, A_buffer.get(), B_buffer.get(), beta, C_buffer.get());
         return;
       }
       const int64_t n = int64_t(size);

@@ -95,6 +95,21 @@ def test_matrix_vector_benchmarks_fp32_only_and_error_report(bench, tmp_path):
     assert len(rows) == 1 and rows[0]["frob_rel"] < 1e-5
 
 
+def test_host_bodies_bitwise_equal_to_per_element_loops(tmp_path):
+    # the vectorised --device=cpu bodies keep each element's reference order
+    import sys
+    sys.path.insert(0, str(ROOT / "sycl-bench_gb300"))
+    import build
+    exe = tmp_path / "host_bodies_check"
+    cmd = ["g++", *build.CXX_FLAGS, "-I", str(build.HARNESS), "-I", str(build.POLY), "-I", str(build.INCLUDE),
+           "-I", str(build.cuda_home() / "include"), str(ROOT / "tests" / "host_bodies_check.cpp"), "-o", str(exe),
+           "-L", str(build.LIB_DIR), "-lgbpoly", f"-Wl,-rpath,{build.LIB_DIR}"]
+    subprocess.run(cmd, check=True, capture_output=True, timeout=300)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    assert r.stdout.count("bitwise equal") == 7 * 7  # 7 sizes x 7 cases
+
+
 def test_stdout_result_names_match_reference():
     ref = (GOLDEN / "reference_stdout_gemm.txt").read_text()
     ours = run("gemm", "--size=16", "--num-runs=3", "--device=cpu", "--precision=fp32").stdout
