@@ -193,16 +193,12 @@ private:
 
   // --device=cpu: the reference kernel bodies (correlation.cpp:115-185) on the host cores
   void host_mean(const float* X, float* mu) const {
-#pragma omp parallel for schedule(static)
-    for(long j = 0; j < long(size); ++j) {
-      for(size_t i = 0; i < size; i++) mu[j] += X[i * ld + j];
-      mu[j] /= ((DATA_TYPE)FLOAT_N);
-    }
+    poly::host_column_sums(size, size, ld, X, mu, [](float x, size_t) { return x; });
+    for(size_t j = 0; j < size; ++j) mu[j] /= ((DATA_TYPE)FLOAT_N);
   }
   void host_std(const float* X, const float* mu, float* sd) const {
-#pragma omp parallel for schedule(static)
-    for(long j = 0; j < long(size); ++j) {
-      for(size_t i = 0; i < size; i++) sd[j] += (X[i * ld + j] - mu[j]) * (X[i * ld + j] - mu[j]);
+    poly::host_column_sums(size, size, ld, X, sd, [mu](float x, size_t j) { return (x - mu[j]) * (x - mu[j]); });
+    for(size_t j = 0; j < size; ++j) {
       sd[j] /= FLOAT_N;
       sd[j] = std::sqrt(sd[j]);
       sd[j] = sd[j] <= EPS ? 1.0 : sd[j];

@@ -155,12 +155,9 @@ private:
 
   // --device=cpu: the reference kernel bodies (covariance.cpp:89-124) on the host cores
   void host_mean(const float* X, float* mu) const {
-#pragma omp parallel for schedule(static)
-    for(long j = 0; j < long(size); ++j) {
-      mu[j] = 0;
-      for(size_t i = 0; i < size; i++) mu[j] += X[i * ld + j];
-      mu[j] /= float_n;
-    }
+    for(size_t j = 0; j < size; ++j) mu[j] = 0;
+    poly::host_column_sums(size, size, ld, X, mu, [](float x, size_t) { return x; });
+    for(size_t j = 0; j < size; ++j) mu[j] /= float_n;
   }
   void host_center(float* X, const float* mu) const {
 #pragma omp parallel for schedule(static)

@@ -408,6 +408,27 @@ inline void host_gemv_t_body(std::size_t n, const float* A, const float* x, floa
   }
 }
 
+// col[j] += term(X[i][j], j) for i = 0..rows-1 in order, each column of an
+// rows x cols X (leading dimension ld): the column means and standard
+// deviations of covariance.cpp:80-96 and correlation.cpp:107-142.  A thread
+// owns a block of 64 columns and walks the rows (contiguous row segments).
+template <class Term>
+void host_column_sums(std::size_t rows, std::size_t cols, std::size_t ld, const float* X, float* col, Term term) {
+  constexpr std::size_t V = 64;
+  const long blocks = long((cols + V - 1) / V);
+#pragma omp parallel for schedule(static)
+  for(long b = 0; b < blocks; ++b) {
+    const std::size_t j0 = std::size_t(b) * V, j1 = std::min(cols, j0 + V);
+    float acc[V];
+    for(std::size_t j = j0; j < j1; j++) acc[j - j0] = col[j];
+    for(std::size_t i = 0; i < rows; i++) {
+      const float* row = X + i * ld;
+      for(std::size_t j = j0; j < j1; j++) acc[j - j0] += term(row[j], j);
+    }
+    for(std::size_t j = j0; j < j1; j++) col[j] = acc[j - j0];
+  }
+}
+
 // S[j1][j2] = S[j2][j1] = sum_i X[i][j1] * X[i][j2] over n x n X (leading
 // dimension ld) for j2 >= j1 + skip, each sum from 0 with i in order: the
 // XᵀX kernels of covariance.cpp:114-126 (skip 0) and correlation.cpp:167-181

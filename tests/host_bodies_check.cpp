@@ -4,6 +4,8 @@
 //   host_syr2k_body            syr2k.cpp:78-87   one statement per k
 //   host_gemv_t_body           atax.cpp:87-95, bicg.cpp:77-84
 //   host_xtx_upper             covariance.cpp:114-126 (skip 0), correlation.cpp:167-181 (skip 1)
+//   host_column_sums           the column means and standard deviations, covariance.cpp:80-96 and
+//                              correlation.cpp:107-142
 // Built with the executables' flags (-O3 -fopenmp -ffp-contract=off); exit
 // status = number of mismatching cases.
 #include <cstdio>
@@ -47,6 +49,12 @@ void loop_xtx(std::size_t n, std::size_t ld, const float* X, float* S, std::size
       for(std::size_t i = 0; i < n; i++) S[j1 * ld + j2] += X[i * ld + j1] * X[i * ld + j2];
       S[j2 * ld + j1] = S[j1 * ld + j2];
     }
+}
+
+void loop_column_sums(std::size_t n, std::size_t ld, const float* X, float* col, const float* mu) {
+  for(std::size_t j = 0; j < n; ++j)
+    for(std::size_t i = 0; i < n; i++)
+      col[j] += mu ? (X[i * ld + j] - mu[j]) * (X[i * ld + j] - mu[j]) : X[i * ld + j];
 }
 
 template <class T>
@@ -97,6 +105,18 @@ int check_columns(std::size_t n) {
     poly::host_xtx_upper(n, ld, X.data() + ld + 1, s2.data() + ld + 1, skip);
     bad += report(skip ? "xtx skip 1" : "xtx skip 0", n, s1.data(), s2.data(), s1.size() * 4);
   }
+  // column sums (means) and squared deviations (standard deviations)
+  const auto mu = normal<float>(n, unsigned(n) + 7);
+  std::vector<float> m1(n, 0.25f), m2(n, 0.25f);
+  loop_column_sums(n, ld, X.data() + ld + 1, m1.data(), nullptr);
+  poly::host_column_sums(n, n, ld, X.data() + ld + 1, m2.data(), [](float v, std::size_t) { return v; });
+  bad += report("column sum", n, m1.data(), m2.data(), n * 4);
+  std::vector<float> d1(n, 0.f), d2(n, 0.f);
+  loop_column_sums(n, ld, X.data() + ld + 1, d1.data(), mu.data());
+  const float* m = mu.data();
+  poly::host_column_sums(n, n, ld, X.data() + ld + 1, d2.data(),
+      [m](float v, std::size_t j) { return (v - m[j]) * (v - m[j]); });
+  bad += report("column dev", n, d1.data(), d2.data(), n * 4);
   return bad;
 }
 
