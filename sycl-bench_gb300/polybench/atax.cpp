@@ -116,11 +116,7 @@ private:
   }
 
   // --device=cpu: the reference kernel bodies (atax.cpp:78-95) on the host cores
-  void host_rows(const float* a, const float* xv, float* t) const {
-#pragma omp parallel for schedule(static)
-    for(long i = 0; i < long(size); ++i)
-      for(size_t j = 0; j < size; j++) t[i] += a[i * size + j] * xv[j];
-  }
+  void host_rows(const float* a, const float* xv, float* t) const { poly::host_gemv_n_body(size, a, xv, t); }
   void host_cols(const float* a, const float* t, float* yv) const { poly::host_gemv_t_body(size, a, t, yv); }
 
   BenchmarkArgs args;

@@ -129,11 +129,7 @@ private:
 
   // --device=cpu: the reference kernel bodies (bicg.cpp:82-98) on the host cores
   void host_cols(const float* a, const float* rv, float* sv) const { poly::host_gemv_t_body(size, a, rv, sv); }
-  void host_rows(const float* a, const float* pv, float* qv) const {
-#pragma omp parallel for schedule(static)
-    for(long i = 0; i < long(size); ++i)
-      for(size_t j = 0; j < size; j++) qv[i] += a[i * size + j] * pv[j];
-  }
+  void host_rows(const float* a, const float* pv, float* qv) const { poly::host_gemv_n_body(size, a, pv, qv); }
 
   BenchmarkArgs args;
   const size_t size;

@@ -127,14 +127,7 @@ private:
   void host_body() {
     const float *a = A_buffer.get(), *b = B_buffer.get(), *xv = x_buffer.get();
     float *t = tmp_buffer.get(), *yv = y_buffer.get();
-#pragma omp parallel for schedule(static)
-    for(long i = 0; i < long(size); ++i) {
-      for(size_t j = 0; j < size; j++) {
-        t[i] += a[i * size + j] * xv[j];
-        yv[i] += b[i * size + j] * xv[j];
-      }
-      yv[i] = ALPHA * t[i] + BETA * yv[i];
-    }
+    poly::host_gesummv_body(size, ALPHA, BETA, a, b, xv, t, yv);
   }
 
   BenchmarkArgs args;

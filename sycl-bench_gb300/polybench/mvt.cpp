@@ -124,11 +124,7 @@ private:
   }
 
   // --device=cpu: the reference kernel bodies (mvt.cpp:80-96) on the host cores
-  void host_rows(const float* av, const float* yv, float* xv) const {
-#pragma omp parallel for schedule(static)
-    for(long i = 0; i < long(size); ++i)
-      for(size_t j = 0; j < size; j++) xv[i] += av[i * size + j] * yv[j];
-  }
+  void host_rows(const float* av, const float* yv, float* xv) const { poly::host_gemv_n_body(size, av, yv, xv); }
 
   BenchmarkArgs args;
   const size_t size;

@@ -408,6 +408,65 @@ inline void host_gemv_t_body(std::size_t n, const float* A, const float* x, floa
   }
 }
 
+// y[i] += A[i][j] * x[j] for an n x n row-major A, j in order for each i:
+// the row kernels of atax.cpp:73-84, bicg.cpp:89-97 and mvt.cpp:75-96.  Each
+// row is a chain of dependent adds, so a thread carries 8 rows at once (8
+// independent chains) instead of waiting on one; every row keeps its order.
+inline void host_gemv_n_body(std::size_t n, const float* A, const float* x, float* y) {
+  constexpr std::size_t R = 8;
+  const long groups = long((n + R - 1) / R);
+#pragma omp parallel for schedule(static)
+  for(long g = 0; g < groups; ++g) {
+    const std::size_t i0 = std::size_t(g) * R;
+    if(i0 + R <= n) {
+      float acc[R];
+      for(std::size_t r = 0; r < R; ++r) acc[r] = y[i0 + r];
+      for(std::size_t j = 0; j < n; ++j) {
+        const float xj = x[j];
+#pragma GCC unroll 8
+        for(std::size_t r = 0; r < R; ++r) acc[r] += A[(i0 + r) * n + j] * xj;
+      }
+      for(std::size_t r = 0; r < R; ++r) y[i0 + r] = acc[r];
+    } else {
+      for(std::size_t i = i0; i < n; ++i)
+        for(std::size_t j = 0; j < n; ++j) y[i] += A[i * n + j] * x[j];
+    }
+  }
+}
+
+// gesummv.cpp:84-98 on the host: tmp[i] += A[i][j] x[j] and y[i] += B[i][j] x[j]
+// with j in order, then y[i] = alpha tmp[i] + beta y[i]; 4 rows per thread at
+// once (8 independent chains), each row in its own order.
+inline void host_gesummv_body(std::size_t n, float alpha, float beta, const float* A, const float* B, const float* x,
+    float* tmp, float* y) {
+  constexpr std::size_t R = 4;
+  const long groups = long((n + R - 1) / R);
+#pragma omp parallel for schedule(static)
+  for(long g = 0; g < groups; ++g) {
+    const std::size_t i0 = std::size_t(g) * R, i1 = std::min(n, i0 + R);
+    if(i1 - i0 == R) {
+      float t[R], u[R];
+      for(std::size_t r = 0; r < R; ++r) t[r] = tmp[i0 + r], u[r] = y[i0 + r];
+      for(std::size_t j = 0; j < n; ++j) {
+        const float xj = x[j];
+#pragma GCC unroll 4
+        for(std::size_t r = 0; r < R; ++r) {
+          t[r] += A[(i0 + r) * n + j] * xj;
+          u[r] += B[(i0 + r) * n + j] * xj;
+        }
+      }
+      for(std::size_t r = 0; r < R; ++r) tmp[i0 + r] = t[r], y[i0 + r] = u[r];
+    } else {
+      for(std::size_t i = i0; i < i1; ++i)
+        for(std::size_t j = 0; j < n; ++j) {
+          tmp[i] += A[i * n + j] * x[j];
+          y[i] += B[i * n + j] * x[j];
+        }
+    }
+    for(std::size_t i = i0; i < i1; ++i) y[i] = alpha * tmp[i] + beta * y[i];
+  }
+}
+
 // col[j] += term(X[i][j], j) for i = 0..rows-1 in order, each column of an
 // rows x cols X (leading dimension ld): the column means and standard
 // deviations of covariance.cpp:80-96 and correlation.cpp:107-142.  A thread

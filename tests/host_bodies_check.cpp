@@ -3,6 +3,8 @@
 //   host_gemm_body(tb = true)  syrk.cpp:74-83    C = beta C + sum_k (alpha A[i][k]) A[j][k]
 //   host_syr2k_body            syr2k.cpp:78-87   one statement per k
 //   host_gemv_t_body           atax.cpp:87-95, bicg.cpp:77-84
+//   host_gemv_n_body           atax.cpp:73-84, bicg.cpp:89-97, mvt.cpp:75-96
+//   host_gesummv_body          gesummv.cpp:84-98
 //   host_xtx_upper             covariance.cpp:114-126 (skip 0), correlation.cpp:167-181 (skip 1)
 //   host_column_sums           the column means and standard deviations, covariance.cpp:80-96 and
 //                              correlation.cpp:107-142
@@ -40,6 +42,22 @@ void loop_syr2k(std::size_t n, T alpha, const T* A, const T* B, T beta, T* C) {
 void loop_gemv_t(std::size_t n, const float* A, const float* x, float* y) {
   for(std::size_t j = 0; j < n; ++j)
     for(std::size_t i = 0; i < n; i++) y[j] += A[i * n + j] * x[i];
+}
+
+void loop_gemv_n(std::size_t n, const float* A, const float* x, float* y) {
+  for(std::size_t i = 0; i < n; ++i)
+    for(std::size_t j = 0; j < n; j++) y[i] += A[i * n + j] * x[j];
+}
+
+void loop_gesummv(std::size_t n, float alpha, float beta, const float* A, const float* B, const float* x, float* tmp,
+    float* y) {
+  for(std::size_t i = 0; i < n; ++i) {
+    for(std::size_t j = 0; j < n; j++) {
+      tmp[i] += A[i * n + j] * x[j];
+      y[i] += B[i * n + j] * x[j];
+    }
+    y[i] = alpha * tmp[i] + beta * y[i];
+  }
 }
 
 void loop_xtx(std::size_t n, std::size_t ld, const float* X, float* S, std::size_t skip) {
@@ -96,6 +114,16 @@ int check_columns(std::size_t n) {
   loop_gemv_t(n, A.data(), x.data(), y1.data());
   poly::host_gemv_t_body(n, A.data(), x.data(), y2.data());
   int bad = report("gemv_t", n, y1.data(), y2.data(), n * 4);
+  y1 = y, y2 = y;
+  loop_gemv_n(n, A.data(), x.data(), y1.data());
+  poly::host_gemv_n_body(n, A.data(), x.data(), y2.data());
+  bad += report("gemv_n", n, y1.data(), y2.data(), n * 4);
+  const auto B = normal<float>(n * n, unsigned(n) + 8), tmp = normal<float>(n, unsigned(n) + 9);
+  auto t1 = tmp, t2 = tmp;
+  y1 = y, y2 = y;
+  loop_gesummv(n, 1.25f, -0.5f, A.data(), B.data(), x.data(), t1.data(), y1.data());
+  poly::host_gesummv_body(n, 1.25f, -0.5f, A.data(), B.data(), x.data(), t2.data(), y2.data());
+  bad += report("gesummv", n, y1.data(), y2.data(), n * 4) + report("gesummv tmp", n, t1.data(), t2.data(), n * 4);
   // X^T X on the interior of an (n+1) x (n+1) array, as covariance/correlation
   const std::size_t ld = n + 1;
   const auto X = normal<float>(ld * ld, unsigned(n) + 6);

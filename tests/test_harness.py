@@ -107,7 +107,7 @@ def test_host_bodies_bitwise_equal_to_per_element_loops(tmp_path):
     subprocess.run(cmd, check=True, capture_output=True, timeout=300)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
-    assert r.stdout.count("bitwise equal") == 7 * 9  # 7 sizes x 9 cases
+    assert r.stdout.count("bitwise equal") == 7 * 12  # 7 sizes x 12 cases
 
 
 def test_stdout_result_names_match_reference():
