@@ -354,7 +354,9 @@ typedef struct {
  * everything once (it allocates the term panels and tables and copies them
  * to the device, synchronously); gbpoly_grouped_run only enqueues launches on
  * the context's stream and can be captured into a graph; the operands and
- * outputs must stay at the addresses given to the plan. */
+ * outputs must stay at the addresses given to the plan.  count = 0 gives an
+ * empty plan (no device memory) whose run launches nothing; fp8 has no
+ * grouped form (GBPOLY_ERR_UNSUPPORTED). */
 typedef struct gbpoly_grouped gbpoly_grouped;
 gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
     gbpoly_grouped** plan);

@@ -1684,9 +1684,16 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
       return fail(GBPOLY_ERR_INVALID, buf);
     }
   }
+  if(prec != GBPOLY_PREC_FP32 && prec != GBPOLY_PREC_BF16X3 && prec != GBPOLY_PREC_TF32X3 &&
+      prec != GBPOLY_PREC_BF16X6 && prec != GBPOLY_PREC_TF32)
+    return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   auto* g = new gbpoly_grouped();
   g->prec = prec;
   g->descs.assign(descs, descs + count);
+  if(count == 0) {  // an empty group: no device memory, running it launches nothing
+    *out = g;
+    return GBPOLY_OK;
+  }
   gbpoly_status st = GBPOLY_OK;
   switch(prec) {
   case GBPOLY_PREC_FP32: {
@@ -1730,6 +1737,7 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
 gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   using namespace gbpoly;
   if(!ctx || !g) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  if(g->descs.empty()) return GBPOLY_OK;
   GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
   switch(g->prec) {
   case GBPOLY_PREC_FP32:

@@ -93,6 +93,19 @@ def test_grouped_run_in_a_graph(ctx):
     ctx.grouped_destroy(plan)
 
 
+@pytest.mark.parametrize("prec", [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.TF32])
+def test_grouped_empty_group(ctx, prec):
+    # an empty group plans without device memory and runs as nothing
+    plan = ctx.grouped_plan(prec, ctx.descs([]))
+    assert ctx.grouped_info(plan) == {"flops": 0, "tiles": 0, "device_bytes": 0}
+    ctx.grouped_run(plan)
+    ctx.synchronize()
+    ctx.grouped_destroy(plan)
+    with pytest.raises(gbpoly.GbpolyError) as e:  # fp8 has no grouped form, empty or not
+        ctx.grouped_plan(Precision.FP8, ctx.descs([]))
+    assert e.value.status == gbpoly.Status.UNSUPPORTED
+
+
 def test_grouped_rejects_bad_descriptor(ctx):
     d = ctx.alloc(64)
     descs = ctx.descs([dict(M=4, N=4, K=4, alpha=1.0, beta=0.0, A=d, lda=2, B=d, ldb=4, C=d, ldc=4)])
