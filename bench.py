@@ -34,8 +34,9 @@ ALPHA, BETA = 32412.0, 2123.0
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 # DRAM bytes (read + write) per launch of the dominant kernel, keyed by
-# (kernel, N, tile configuration), from one ncu capture of the same kernel,
-# configuration and workload (profiles/split_gemm_bf16x3_n4096_n8192.md).
+# (kernel, N, tile configuration): ncu's dram__bytes_read.sum +
+# dram__bytes_write.sum from one capture of the same kernel, configuration
+# and workload.
 TRAFFIC_PER_LAUNCH: dict[tuple[str, int, int], float] = {
     ("bf16x3_gemm", 4096, 1): 397.3e6, ("bf16x3_gemm", 8192, 1): 2.797e9,
     ("bf16x3_gemm", 4096, 3): 462.6e6, ("bf16x3_gemm", 8192, 3): 3.163e9}
@@ -58,6 +59,79 @@ def load_peaks() -> tuple[dict, str]:
         except (OSError, ValueError):
             pass
     return dict(FALLBACK_PEAKS), "fallback"
+
+
+class NvmlSampler:
+    """SM clock, its maximum, power and clock-event reasons read through NVML
+    (the driver's libnvidia-ml, read-only queries) every 5 ms in a thread, so
+    that a timed region of a few tens of milliseconds still holds samples.
+    The device is found by its PCI bus id, as the CUDA runtime reports it."""
+
+    # nvmlClocksEventReason bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, device: int, period_s: float = 0.005):
+        import ctypes as ct
+        self.ct = ct
+        self.period = period_s
+        self.samples: list[tuple[float, float, float, int, float]] = []
+        self.stop_flag = threading.Event()
+        self.thread = None
+        self.nvml = ct.CDLL("libnvidia-ml.so.1")
+        if self.nvml.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        rt = ct.CDLL("libcudart.so.13")
+        bus = ct.create_string_buffer(64)
+        if rt.cudaDeviceGetPCIBusId(bus, 64, device) != 0:
+            raise OSError("cudaDeviceGetPCIBusId failed")
+        self.handle = ct.c_void_p()
+        if self.nvml.nvmlDeviceGetHandleByPciBusId_v2(bus, ct.byref(self.handle)) != 0:
+            raise OSError("nvmlDeviceGetHandleByPciBusId failed")
+        self.reasons_fn = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def _one(self):
+        ct = self.ct
+        sm, smax, mw, rs = ct.c_uint(), ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        ok = self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, ct.byref(sm)) == 0  # NVML_CLOCK_SM
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, 1, ct.byref(smax))
+        self.nvml.nvmlDeviceGetPowerUsage(self.handle, ct.byref(mw))
+        self.reasons_fn(self.handle, ct.byref(rs))
+        if ok:
+            self.samples.append((time.time(), float(sm.value), float(smax.value), int(rs.value), mw.value / 1e3))
+
+    def _run(self):
+        while not self.stop_flag.is_set():
+            self._one()
+            time.sleep(self.period)
+
+    def start(self) -> None:
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> None:
+        self.stop_flag.set()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float) -> dict:
+        rows = [s for s in self.samples if t0 <= s[0] <= t1]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no NVML sample in the timed region"],
+                    "samples": 0}
+        reasons = sorted({name for r in rows for bit, name in self.REASONS.items() if r[3] & bit})
+        return {"sm_mhz": statistics.median(r[1] for r in rows), "sm_max_mhz": max(r[2] for r in rows),
+                "sm_mhz_min": min(r[1] for r in rows), "reasons": reasons, "samples": len(rows),
+                "window": f"timed region ({t1 - t0:.3f} s), NVML every {self.period * 1e3:.0f} ms",
+                "power_w_max": max(r[4] for r in rows)}
+
+
+def clock_sampler(device: int):
+    """NVML sampler when the driver library answers, else nvidia-smi every 200 ms."""
+    try:
+        return NvmlSampler(device)
+    except (OSError, AttributeError):
+        return ClockSampler(device)
 
 
 class ClockSampler:
@@ -187,7 +261,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     forms = [Precision[f.strip().upper()] for f in args.forms.split(",")]
     headline = Precision.BF16X3 if Precision.BF16X3 in forms else forms[-1]
     tiers = {}
-    sampler = ClockSampler(dist.local_rank)
+    sampler = clock_sampler(dist.local_rank)
     sampler.start()
     timed_window = (0.0, 0.0)
     tuned = {}
@@ -228,25 +302,35 @@ def run_gpu(args, dist: Dist) -> dict | None:
         ctx.synchronize()
         max_rel, frob, elem = ctx.error_norms(dC, n, dR, n, n, n)
         for _ in range(args.warmup):
+            fresh_c()
             one(prec)
         ctx.synchronize()
-        ev0, ev1 = ctx.event(), ctx.event()
+        # Every timed step starts from the initial C (a device copy between the
+        # step's events, outside them), so each step computes the benchmark's own
+        # output and the last one is checked against FP64 below; each step is
+        # bracketed by its own event pair.
+        evs = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
         dist.barrier()
         ctx.synchronize()
         ctx.profile_read()  # drop records of earlier launches
         ctx.profile(True)
         t0 = time.time()
-        ev0.record()
-        for _ in range(args.steps):
+        for s0, s1 in evs:
+            fresh_c()
+            s0.record()
             one(prec)
-        ev1.record()
+            s1.record()
         ctx.synchronize()
         t1 = time.time()
         ctx.profile(False)
         kernels = ctx.profile_read()
         dist.barrier()
-        ms = ev0.elapsed_ms(ev1) / args.steps
+        ms = sum(s0.elapsed_ms(s1) for s0, s1 in evs) / args.steps
+        for s0, s1 in evs:
+            s0.destroy()
+            s1.destroy()
         ms = dist.max(ms)
+        timed_err = ctx.error_norms(dC, n, dR, n, n, n)
         if prec == headline:
             timed_window = (t0, t1)
         top = max(kernels.items(), key=lambda kv: kv[1][1])
@@ -259,9 +343,8 @@ def run_gpu(args, dist: Dist) -> dict | None:
                         for k, (c, t) in kernels.items()},
             "dominant_kernel": top[0], "dominant_avg_ms": top[1][1] / top[1][0],
             "tile_config": tuned.get(prec),
+            "timed_output_err_vs_fp64": {"max_rel": timed_err[0], "frob_rel": timed_err[1]},
         }
-        ev0.destroy()
-        ev1.destroy()
     sampler.stop()
     clocks = sampler.summary(*timed_window)
 
@@ -291,6 +374,32 @@ def run_gpu(args, dist: Dist) -> dict | None:
     e1.record()
     ctx.synchronize()
     e2e_ms = dist.max(e0.elapsed_ms(e1) / args.steps)
+    # the host link on this machine, measured now: plain copies between the same pinned
+    # buffers and device memory, one direction at a time
+    dtmp = ctx.alloc(nbytes)
+
+    def copy_ms(h2d: bool, reps: int = 5) -> float:
+        for _ in range(2):
+            for hp in (hA, hB, hC):
+                (ctx.lib.gbpoly_memcpy_h2d(ctx.handle, gbpoly._ptr(dtmp), ct.c_void_p(hp), nbytes) if h2d else
+                 ctx.lib.gbpoly_memcpy_d2h(ctx.handle, ct.c_void_p(hp), gbpoly._ptr(dtmp), nbytes))
+        ctx.synchronize()
+        c0, c1 = ctx.event(), ctx.event()
+        c0.record()
+        for _ in range(reps):
+            for hp in (hA, hB, hC):
+                gbpoly._check(ctx.lib.gbpoly_memcpy_h2d(ctx.handle, gbpoly._ptr(dtmp), ct.c_void_p(hp), nbytes) if h2d
+                              else ctx.lib.gbpoly_memcpy_d2h(ctx.handle, ct.c_void_p(hp), gbpoly._ptr(dtmp), nbytes))
+        c1.record()
+        ctx.synchronize()
+        return c0.elapsed_ms(c1) / (3 * reps)
+    h2d_gbs = nbytes / (copy_ms(True) * 1e-3) / 1e9
+    d2h_gbs = nbytes / (copy_ms(False) * 1e-3) / 1e9
+    ctx.free(dtmp)
+    h2d_only_ms = 3 * nbytes / (h2d_gbs * 1e9) * 1e3
+    link = {"h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs,
+            "h2d_bytes_alone_ms": h2d_only_ms, "e2e_frac_of_h2d_bound": h2d_only_ms / e2e_ms,
+            "measured": "plain pinned cudaMemcpyAsync of N^2 x 4 B, same buffers, same run, one direction at a time"}
     for p in (hA, hB, hC):
         ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
 
@@ -327,11 +436,37 @@ def run_gpu(args, dist: Dist) -> dict | None:
         "value": head["tflops"], "ms_per_step": head["ms_per_step"], "tiers": tiers, "clocks": clocks,
         "roofline": roof, "headline": headline.name.lower(),
         "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 * dist.world, "unit": "TFLOP/s",
-                "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms},
+                "h2d_bytes_per_step": 3 * nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms,
+                "link": link},
+        "err_vs_fp64": {"form": headline.name.lower(), "polybench_inputs": head["err_vs_fp64"],
+                        "uniform_inputs": head["err_vs_fp64_uniform_inputs"],
+                        "timed_output": head["timed_output_err_vs_fp64"]},
+        "matched_error": matched_error(tiers),
         "gpu_launches": int(round(args.steps * head["kernel_launches_per_step"])),
         "device": props, "peak_kind": peak_kind, "grouped": grouped, "family": family,
         "neighbours": neighbours, "small_k": small_k,
     }
+
+
+def matched_error(tiers: dict) -> dict | None:
+    """The fastest tensor-core form whose normwise and Frobenius errors against
+    FP64 are both no larger than plain FP32's, on the polybench and on the
+    uniform[-1, 1] inputs, with its throughput over FP32's."""
+    f32 = tiers.get("fp32")
+    if not f32:
+        return None
+
+    def within(t):
+        return all(t[key][m] <= f32[key][m] for key in ("err_vs_fp64", "err_vs_fp64_uniform_inputs")
+                   for m in ("max_rel", "frob_rel"))
+    ok = {name: t for name, t in tiers.items() if name != "fp32" and within(t)}
+    out = {"criterion": "max-normwise and Frobenius error vs FP64 <= plain FP32's, polybench and uniform[-1,1] "
+                        "inputs, same N",
+           "forms_meeting_it": sorted(ok), "fp32_tflops": f32["tflops"]}
+    if ok:
+        best = max(ok, key=lambda k: ok[k]["tflops"])
+        out.update(form=best, tflops=ok[best]["tflops"], vs_fp32=ok[best]["tflops"] / f32["tflops"])
+    return out
 
 
 def run_family(ctx, args) -> dict:
@@ -971,7 +1106,8 @@ def main() -> None:
     n = args.size
     config = {"workload": f"polybench gemm C=alpha*A*B+beta*C, N={n} (NI=NJ=NK), alpha=32412, beta=2123, "
                           f"polybench init A=i*k/N B=(k*j+1)/N C=(i*j+2)/N",
-              "size": n, "flops_per_step": 2 * n ** 3, "l2": "inputs larger than L2 (3 x N^2 x 4 B), no flush",
+              "size": n, "flops_per_step": 2 * n ** 3, "l2": "inputs larger than L2 (3 x N^2 x 4 B), no flush; C restored from its initial copy before "
+                                "every step, outside the step's events",
               "parallelism": f"replicas x{dist.world}"}
     base = {"metric": "GEMM-family TFLOP/s (split-BF16 tcgen05 vs plain FP32 SIMT, matched FP64 error)",
             "unit": "TFLOP/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
@@ -1010,6 +1146,7 @@ def main() -> None:
         line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"],
                     dtype="f32" if res["headline"] == "fp32" else "bf16x3 (f32 in/out, bf16 hi/lo products, f32 accumulate)",
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
+                    err_vs_fp64=res["err_vs_fp64"], matched_error=res["matched_error"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],
                     device={"sm_count": res["device"]["sm_count"], "cc": list(res["device"]["cc"])},
                     peaks=res["peak_kind"], grouped=res["grouped"], family=res["family"],

@@ -369,8 +369,11 @@ gbpoly_status gbpoly_grouped_destroy(gbpoly_ctx* ctx, gbpoly_grouped* plan);
 gbpoly_status gbpoly_gemm_grouped_f32(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
     int count);
 
-/* Allocation-free split-BF16 contraction: the same result as
- * gbpoly_gemm_f32(ctx, GBPOLY_PREC_BF16X3, ...), for callers that may not
+/* Allocation-free split-BF16 contraction: the same contraction as
+ * gbpoly_gemm_f32(ctx, GBPOLY_PREC_BF16X3, ...), within split-BF16 rounding
+ * (it always runs the fixed 1-CTA 128 x 256 tile configuration 0 over whole
+ * tiles: no autotuned choice, no K-split tail, no lower-triangle mirroring,
+ * so the sums may round differently), for callers that may not
  * allocate device memory at call time (graph capture in global mode, an
  * application-owned memory pool, allocation-free real-time loops, device
  * memory quotas).  It has no counterpart in the reference.
@@ -380,7 +383,10 @@ gbpoly_status gbpoly_gemm_grouped_f32(gbpoly_ctx* ctx, gbpoly_precision prec, co
  *   - shapes whose panels exceed it, about (M + N) * round_up(K, 64) * 4 bytes
  *     > 32 MiB, are rejected with GBPOLY_ERR_INVALID and a message;
  *   - the first call on each device looks the array's device address up
- *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     The address belongs to the device's context: after cudaDeviceReset
+ *     (or anything else that replaces the context) the next call looks it up
+ *     again, so make that call outside stream capture too;
  *   - all calls share the one array: calls whose work overlaps on the GPU
  *     (several streams or contexts on one device) race and must be ordered
  *     by the caller. */

@@ -1814,21 +1814,59 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 
-// Device address of g_noalloc_scratch, looked up once per device with that
-// device current (the array's name is only a host-side handle in host code).
+// Device address of g_noalloc_scratch, looked up with the device current
+// (the array's name is only a host-side handle in host code).  The address
+// belongs to the device's context: the cache remembers which context it was
+// read in and reads it again when the current context differs, as it does
+// after cudaDeviceReset has torn the old one down and the module has been
+// loaded into a new one.
 std::mutex g_noalloc_mutex;
-void* g_noalloc_addr[64] = {};
+struct NoAllocAddr {
+  unsigned long long ctx_id = 0;
+  void* ptr = nullptr;
+};
+NoAllocAddr g_noalloc_addr[64];
+
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Process-unique id of the calling thread's current context (cuCtxGetId), 0
+// when the driver does not report one.
+unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static bool resolved = false;
+  if(!resolved) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PfnCtxGetCurrent>(fn);
+    fn = nullptr;
+    if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(fn);
+    resolved = true;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if(!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 gbpoly_status noalloc_scratch(int device, char** out) {
   if(device < 0 || device >= 64) return fail(GBPOLY_ERR_UNSUPPORTED, "device index beyond 63");
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if(!g_noalloc_addr[device]) {
+  NoAllocAddr& slot = g_noalloc_addr[device];
+  const unsigned long long id = current_context_id();
+  if(!slot.ptr || (id != 0 && id != slot.ctx_id)) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if(e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-    g_noalloc_addr[device] = p;
+    slot.ptr = p;
+    slot.ctx_id = id;
   }
-  *out = static_cast<char*>(g_noalloc_addr[device]);
+  *out = static_cast<char*>(slot.ptr);
   return GBPOLY_OK;
 }
 

@@ -26,8 +26,10 @@ def test_2mm_graph_replay_matches_eager(ctx, prec):
     eager = ctx.download(dE, (n, n))
     ctx.workspace_reserve(ctx.workspace_query(prec, n, n, n))
     ctx.graph_begin()
-    stages()
-    g = ctx.graph_end()
+    try:
+        stages()
+    finally:
+        g = ctx.graph_end()  # a failed call must not leave the stream capturing
     for _ in range(2):  # replay twice, C reset in between (stage 1 accumulates into C)
         ctx.h2d(dC, C)
         ctx.graph_launch(g)
@@ -37,13 +39,16 @@ def test_2mm_graph_replay_matches_eager(ctx, prec):
     assert oracle.verify(oracle.host_mm2(n), eager)[0] == -1
 
 
-def test_workspace_growth_during_capture_is_refused(ctx):
-    n = 2048 + 64  # larger than anything reserved before in this session
-    d = ctx.alloc(n * n * 4)
-    ctx.graph_begin()
-    with pytest.raises(gbpoly.GbpolyError) as e:
-        ctx.gemm(Precision.BF16X6, n, n, n, 1.0, d, n, d, n, 0.0, d, n)
-    assert e.value.status == gbpoly.Status.STATE
-    g = ctx.graph_end()  # nothing was enqueued: an empty graph
-    ctx.graph_destroy(g)
-    ctx.synchronize()
+def test_workspace_growth_during_capture_is_refused():
+    n = 2048 + 64
+    with gbpoly.Context(0) as fresh:  # its workspace is empty: any tensor-core call must grow it
+        d = fresh.alloc(n * n * 4)
+        fresh.graph_begin()
+        try:
+            with pytest.raises(gbpoly.GbpolyError) as e:
+                fresh.gemm(Precision.BF16X6, n, n, n, 1.0, d, n, d, n, 0.0, d, n)
+        finally:
+            g = fresh.graph_end()  # nothing was enqueued: an empty graph
+            fresh.graph_destroy(g)
+        assert e.value.status == gbpoly.Status.STATE
+        fresh.synchronize()

@@ -81,8 +81,10 @@ def test_grouped_run_in_a_graph(ctx):
     ctx.synchronize()
     eager = [ctx.download(b[2], (p[2], p[3])) for p, b in zip(probs, bufs)]
     ctx.graph_begin()
-    ctx.grouped_run(plan)
-    g = ctx.graph_end()
+    try:
+        ctx.grouped_run(plan)
+    finally:
+        g = ctx.graph_end()  # a failed call must not leave the stream capturing
     for p, b in zip(probs, bufs):
         ctx.h2d(b[2], p[7])  # restore C (beta = 0.5 reads it)
     ctx.graph_launch(g)

@@ -74,12 +74,16 @@ def test_gemm_random_ops_vs_fp64(ctx, prec, op_a, op_b, mnk):
     assert frob < frob_bound(prec, K), (max_rel, frob)
 
 
+BF16X3_RATIO = 10.0
+
+
 def test_error_relative_to_fp32(ctx):
     """Error against the FP64 oracle relative to plain FP32's, normal(0,1) inputs.
 
     tf32x3 and bf16x6 keep ~24 significand bits per operand and match FP32;
-    bf16x3 keeps ~16 and is about ten times worse (still 100x inside the
-    0.05 percent verify threshold)."""
+    bf16x3 keeps ~16: at K = 512 its Frobenius error is BF16X3_RATIO times
+    FP32's as measured on a GB300 (still 100x inside the 0.05 percent verify
+    threshold), and the test allows 1.5 times that ratio."""
     n = 512
     rng = np.random.default_rng(3)
     A = rng.standard_normal((n, n)).astype(np.float32)
@@ -92,7 +96,7 @@ def test_error_relative_to_fp32(ctx):
     f32 = err[Precision.FP32]
     assert err[Precision.TF32X3] < 1.5 * f32
     assert err[Precision.BF16X6] < 1.5 * f32
-    assert err[Precision.BF16X3] < 30 * f32
+    assert err[Precision.BF16X3] < 1.5 * BF16X3_RATIO * f32
 
 
 @pytest.mark.parametrize("prec", [Precision.TF32X3, Precision.BF16X6])

@@ -1,12 +1,21 @@
 """The allocation-free split-BF16 entry point, through the C ABI.
 
 gbpoly_gemm_f32_bf16x3_noalloc serves callers that may not allocate device
-memory at call time: it keeps its split panels in a fixed device array
-inside the library instead of the context workspace.  Two calls in a row, of
-different shapes (the second must not see the first one's panels), must give
-what the existing entry point gbpoly_gemm_f32(..., GBPOLY_PREC_BF16X3, ...)
-gives, within the split-BF16 tolerance of the other tests (Frobenius 2e-5);
-a shape whose panels do not fit is refused with a message.
+memory when they call a contraction: code captured into a CUDA graph in
+global mode, applications whose memory pool owns the whole device, real-time
+loops that forbid the synchronisation an allocation can cause, processes
+under a device-memory quota.  It keeps its split panels in a fixed device
+array inside the library instead of the context workspace.
+
+Two calls in a row, of different shapes (the second must not see the first
+one's panels), on a context that has never run a contraction:
+  * give what the existing entry point gbpoly_gemm_f32(..., GBPOLY_PREC_BF16X3,
+    ...) gives, within the split-BF16 tolerance of the other tests
+    (Frobenius 2e-5), and are within that tolerance of the FP64 oracle too;
+  * leave the device's free memory exactly as it was (after one warm-up call
+    of each shape, which looks the array's address up and loads the kernels):
+    neither call allocated.
+A shape whose panels do not fit is refused with a message.
 
 The file name sorts last so that a run stopping at its first failure has
 already run every other test.
@@ -17,6 +26,7 @@ import numpy as np
 import pytest
 
 import gbpoly
+import oracle
 from gbpoly import Op, Precision
 
 pytestmark = pytest.mark.gpu
@@ -25,46 +35,79 @@ TOL = 2e-5
 
 
 def frob_rel(x, ref):
-    return float(np.linalg.norm(x.astype(np.float64) - ref) / max(np.linalg.norm(ref.astype(np.float64)), 1e-300))
+    ref = ref.astype(np.float64)
+    return float(np.linalg.norm(x.astype(np.float64) - ref) / max(np.linalg.norm(ref), 1e-300))
+
+
+def device_free_bytes() -> int:
+    """cudaMemGetInfo's free bytes of the current device (the CUDA runtime the library loaded)."""
+    rt = ct.CDLL("libcudart.so.13")
+    free, total = ct.c_size_t(), ct.c_size_t()
+    assert rt.cudaMemGetInfo(ct.byref(free), ct.byref(total)) == 0
+    return free.value
 
 
 def call_noalloc(ctx, op_a, op_b, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc) -> int:
     fn = ctx.lib.gbpoly_gemm_f32_bf16x3_noalloc
-    return fn(ctx.handle, int(op_a), int(op_b), M, N, K, ct.c_float(alpha), ct.c_void_p(dA.ptr), lda,
-              ct.c_void_p(dB.ptr), ldb, ct.c_float(beta), ct.c_void_p(dC.ptr), ldc)
+    return fn(ctx.handle, int(op_a), int(op_b), M, N, K, ct.c_float(alpha), ct.c_void_p(int(dA)), lda,
+              ct.c_void_p(int(dB)), ldb, ct.c_float(beta), ct.c_void_p(int(dC)), ldc)
 
 
-def both_paths(ctx, A, B, C, alpha, beta, op_a, op_b):
+def shape_of(A, B, op_a, op_b):
     M = A.shape[1] if op_a == Op.T else A.shape[0]
     K = A.shape[0] if op_a == Op.T else A.shape[1]
     N = B.shape[0] if op_b == Op.T else B.shape[1]
-    dA, dB = ctx.upload(A), ctx.upload(B)
-    d_ref, d_new = ctx.upload(C), ctx.upload(C)
-    ctx.gemm(Precision.BF16X3, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, d_ref, N, op_a=op_a, op_b=op_b)
-    status = call_noalloc(ctx, op_a, op_b, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, d_new, N)
-    assert status == 0, ctx.lib.gbpoly_last_error()
-    ctx.synchronize()
-    ref = ctx.download(d_ref, C.shape)
-    new = ctx.download(d_new, C.shape)
-    for b in (dA, dB, d_ref, d_new):
+    return M, N, K
+
+
+def workspace_result(ctx, case):
+    """The existing entry point's result (it allocates its workspace as it needs)."""
+    A, B, C, alpha, beta, op_a, op_b = case
+    M, N, K = shape_of(A, B, op_a, op_b)
+    dA, dB, dC = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+    ctx.gemm(Precision.BF16X3, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, dC, N, op_a=op_a, op_b=op_b)
+    out = ctx.download(dC, C.shape)
+    for b in (dA, dB, dC):
         ctx.free(b)
-    return ref, new
+    return out
 
 
-def test_two_calls_match_the_workspace_entry_point(ctx):
+def test_two_calls_match_and_allocate_nothing(ctx):
     rng = np.random.default_rng(11)
-    # call 1: 1024 x 1024 x 1024, both operands as stored
-    A = rng.standard_normal((1024, 1024)).astype(np.float32)
-    B = rng.standard_normal((1024, 1024)).astype(np.float32)
-    C = rng.standard_normal((1024, 1024)).astype(np.float32)
-    ref, new = both_paths(ctx, A, B, C, 1.5, -0.5, Op.N, Op.N)
-    assert frob_rel(new, ref) < TOL
-    # call 2: a smaller, ragged shape with B transposed; stale panels of call 1 must not leak in
-    A2 = rng.uniform(-1, 1, (300, 1000)).astype(np.float32)
-    B2 = rng.uniform(-1, 1, (200, 1000)).astype(np.float32)
-    C2 = rng.uniform(-1, 1, (300, 200)).astype(np.float32)
-    ref2, new2 = both_paths(ctx, A2, B2, C2, 2.0, 0.25, Op.N, Op.T)
-    assert frob_rel(new2, ref2) < TOL
+    cases = [
+        # 1024 x 1024 x 1024, both operands as stored
+        (rng.standard_normal((1024, 1024)).astype(np.float32), rng.standard_normal((1024, 1024)).astype(np.float32),
+         rng.standard_normal((1024, 1024)).astype(np.float32), 1.5, -0.5, Op.N, Op.N),
+        # a smaller, ragged shape with B transposed: stale panels of the first call must not leak in
+        (rng.uniform(-1, 1, (300, 1000)).astype(np.float32), rng.uniform(-1, 1, (200, 1000)).astype(np.float32),
+         rng.uniform(-1, 1, (300, 200)).astype(np.float32), 2.0, 0.25, Op.N, Op.T),
+    ]
+    refs = [workspace_result(ctx, c) for c in cases]
+    f64 = [oracle.gemm_f64(A, B, C, alpha, beta, op_a=int(op_a), op_b=int(op_b))
+           for A, B, C, alpha, beta, op_a, op_b in cases]
+
+    with gbpoly.Context(0) as fresh:  # never ran a contraction: an empty workspace
+        dev = []
+        for A, B, C, alpha, beta, op_a, op_b in cases:
+            dev.append((fresh.upload(A), fresh.upload(B), fresh.alloc(C.nbytes)))
+
+        def run_all():
+            for (A, B, C, alpha, beta, op_a, op_b), (dA, dB, dC) in zip(cases, dev):
+                fresh.h2d(dC, C)
+                M, N, K = shape_of(A, B, op_a, op_b)
+                status = call_noalloc(fresh, op_a, op_b, M, N, K, alpha, dA, A.shape[1], dB, B.shape[1], beta, dC, N)
+                assert status == 0, fresh.lib.gbpoly_last_error()
+            fresh.synchronize()
+
+        run_all()  # warm-up: the first call looks the array's address up
+        free_before = device_free_bytes()
+        run_all()  # the two calls under test
+        free_after = device_free_bytes()
+        outs = [fresh.download(dC, C.shape) for (_, _, C, *_), (_, _, dC) in zip(cases, dev)]
+    assert free_after == free_before, f"device free memory changed by {free_before - free_after} bytes"
+    for out, ref, r64 in zip(outs, refs, f64):
+        assert frob_rel(out, ref) < TOL
+        assert frob_rel(out, r64) < TOL
 
 
 def test_oversized_shape_is_refused(ctx):
