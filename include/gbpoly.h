@@ -175,6 +175,27 @@ gbpoly_status gbpoly_graph_destroy(gbpoly_ctx* ctx, gbpoly_graph* graph);
 gbpoly_status gbpoly_stream_hold(gbpoly_ctx* ctx, uint32_t timeout_us);
 gbpoly_status gbpoly_stream_release(gbpoly_ctx* ctx);
 
+/* ------------------------------------------------------------ diagnostics -- */
+/* Failure paths, exercised without any fault on the GPU.
+ *
+ * gbpoly_wait_probe queues one small kernel whose bounded wait, made by the
+ * same routine as every pipeline wait of the contraction kernels, is on an
+ * mbarrier that nothing completes: after limit_us it records its code in the
+ * context's error word and returns.  The next gbpoly_synchronize then returns
+ * GBPOLY_ERR_TIMEOUT (and clears the word), exactly as it does when a
+ * kernel's pipeline stalls past its 2 s limit, and the context stays usable.
+ * This is the device side of the error the reference throws from
+ * queue::wait_and_throw() and catches per benchmark (include/common.h:61,
+ * :208-212).
+ *
+ * Host-side fault injection (environment variable GBPOLY_FAULT_INJECT, read
+ * by gbpoly_init): "alloc:N" makes the N-th later gbpoly_malloc of the
+ * process return GBPOLY_ERR_NOMEM without allocating; "corrupt:N" changes the
+ * first 4 bytes of the destination of the N-th later gbpoly_memcpy_d2h once
+ * the copy has landed (a float v becomes 2v + 1), so a caller's verification
+ * sees a wrong element.  Unset, it injects nothing. */
+gbpoly_status gbpoly_wait_probe(gbpoly_ctx* ctx, uint32_t limit_us);
+
 /* ----------------------------------------------------------------- events -- */
 
 /* Event handles for kernel-time profiling.  They replace the
@@ -363,6 +384,30 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
 gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* plan);
 /* Algorithmic FLOPs (sum of 2MNK), output tiles and device bytes of a plan. */
 gbpoly_status gbpoly_grouped_info(gbpoly_grouped* plan, int64_t* flops, int* tiles, size_t* device_bytes);
+/* The tile configuration a plan runs. */
+gbpoly_status gbpoly_grouped_config_of(gbpoly_grouped* plan, int* config);
+
+/* Tile configurations of grouped plans (the tile shape, cluster size and
+ * pipeline depth of the persistent grouped kernel): 0 = 1-CTA 128 x 128
+ * tiles, 3 stages of 128 bytes of K (bf16x6: 4 stages of 64 bytes); 1 = CTA
+ * pairs on 256 x 256 tiles (cta_group::2); bf16x3 also 2 = 1-CTA 128 x 256
+ * tiles, 2 stages.  The context keeps one per problem class: the form and
+ * ceil(log2) of the problem count and of the median M, N and K.  Untuned, a
+ * class uses 1 when its 256 x 256 tiles pad the work at most 5 % more than
+ * 128 x 128 tiles and fill every SM pair at least once, else 0.
+ * gbpoly_autotune_grouped plans and runs the group with every configuration
+ * (`reps` timed runs each, on the caller's operands: C is overwritten), keeps
+ * the fastest for the group's class and returns it; gbpoly_autotune_save /
+ * _load persist these entries with the single-contraction ones.  There is no
+ * such tuner in the reference, whose stages (e.g. 3mm.cpp:115-158) are fixed
+ * separate kernels. */
+gbpoly_status gbpoly_grouped_config_count(gbpoly_precision prec, int* count);
+gbpoly_status gbpoly_grouped_config_set(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int config);
+gbpoly_status gbpoly_grouped_config_get(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int* config);
+gbpoly_status gbpoly_autotune_grouped(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int reps, int* best_config, float* best_ms);
 /* Waits for the context's stream, then frees the plan. */
 gbpoly_status gbpoly_grouped_destroy(gbpoly_ctx* ctx, gbpoly_grouped* plan);
 /* Plan, run and destroy in one call (synchronous). */

@@ -2,8 +2,10 @@
 // points declared in include/gbpoly.h.  Argument checking lives here; the
 // kernels live in their own translation units.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <string>
 
 #include "gbpoly_internal.cuh"
@@ -108,6 +110,60 @@ __global__ void hold_kernel(const volatile unsigned* word, unsigned value, uint6
   }
 }
 
+// gbpoly_wait_probe: one bounded wait, through the kernels' own wait
+// routine, on an mbarrier whose phase nothing completes.  It runs out after
+// limit_ns, records kDevErrProbeWait in the error word and returns, as a
+// kernel whose pipeline stalled does; no copy or MMA is in flight.
+__global__ void wait_probe_kernel(int* err, uint64_t limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if(threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) mbar_wait_for(&bar, 0, err, kDevErrProbeWait, limit_ns);
+  __syncthreads();
+}
+
+// ------------------------------------------------------ host fault injection
+// GBPOLY_FAULT_INJECT, read when a context is created, makes one host-side
+// call fail or misbehave so that callers can test their error paths without
+// any fault on the GPU:
+//   alloc:N    the N-th later gbpoly_malloc (process-wide) returns
+//              GBPOLY_ERR_NOMEM without calling cudaMalloc;
+//   corrupt:N  after the N-th later gbpoly_memcpy_d2h has landed, a host
+//              callback on the stream changes the first 4 bytes of its
+//              destination (read as a float v, written as 2v + 1).
+// Unset (or any other value) clears a pending injection.
+namespace {
+std::atomic<long> g_inject_alloc{0}, g_inject_corrupt{0};
+
+void read_fault_injection() {
+  g_inject_alloc = 0;
+  g_inject_corrupt = 0;
+  const char* v = getenv("GBPOLY_FAULT_INJECT");
+  if(!v) return;
+  long n = 0;
+  if(sscanf(v, "alloc:%ld", &n) == 1 && n > 0) g_inject_alloc = n;
+  else if(sscanf(v, "corrupt:%ld", &n) == 1 && n > 0) g_inject_corrupt = n;
+}
+
+// true exactly once: when the countdown steps from 1 to 0
+bool inject_now(std::atomic<long>& countdown) {
+  long c = countdown.load();
+  while(c > 0)
+    if(countdown.compare_exchange_weak(c, c - 1)) return c == 1;
+  return false;
+}
+
+void CUDART_CB corrupt_first_float(void* p) {
+  float v;
+  memcpy(&v, p, sizeof v);
+  v = 2.0f * v + 1.0f;
+  memcpy(p, &v, sizeof v);
+}
+}  // namespace
+
 }  // namespace gbpoly
 
 using namespace gbpoly;
@@ -154,6 +210,7 @@ const char* gbpoly_last_error(void) { return last_error_cstr(); }
 gbpoly_status gbpoly_init(int device, gbpoly_ctx** out_ctx) {
   if(!out_ctx) return fail(GBPOLY_ERR_INVALID, "null output pointer");
   *out_ctx = nullptr;
+  read_fault_injection();
   int count = 0;
   GBPOLY_CUDA_TRY(cudaGetDeviceCount(&count));
   if(device < 0 || device >= count) return fail(GBPOLY_ERR_INVALID, "device index out of range");
@@ -362,6 +419,8 @@ gbpoly_status gbpoly_malloc(gbpoly_ctx* ctx, void** dptr, size_t bytes) {
   if(!dptr) return fail(GBPOLY_ERR_INVALID, "null output pointer");
   *dptr = nullptr;
   if(bytes == 0) return GBPOLY_OK;
+  if(inject_now(g_inject_alloc))
+    return fail(GBPOLY_ERR_NOMEM, "cudaMalloc(dptr, bytes): allocation failure injected by GBPOLY_FAULT_INJECT");
   GBPOLY_CUDA_TRY(cudaMalloc(dptr, bytes));
   return GBPOLY_OK;
 }
@@ -399,7 +458,10 @@ gbpoly_status gbpoly_memcpy_h2d(gbpoly_ctx* ctx, void* dst, const void* src, siz
   return copy(ctx, dst, src, bytes, cudaMemcpyHostToDevice);
 }
 gbpoly_status gbpoly_memcpy_d2h(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  return copy(ctx, dst, src, bytes, cudaMemcpyDeviceToHost);
+  gbpoly_status st = copy(ctx, dst, src, bytes, cudaMemcpyDeviceToHost);
+  if(st == GBPOLY_OK && bytes >= sizeof(float) && inject_now(g_inject_corrupt))
+    GBPOLY_CUDA_TRY(cudaLaunchHostFunc(ctx->stream, corrupt_first_float, dst));
+  return st;
 }
 gbpoly_status gbpoly_memcpy_d2d(gbpoly_ctx* ctx, void* dst, const void* src, size_t bytes) {
   return copy(ctx, dst, src, bytes, cudaMemcpyDeviceToDevice);
@@ -454,6 +516,13 @@ gbpoly_status gbpoly_stream_hold(gbpoly_ctx* ctx, uint32_t timeout_us) {
   CTX_TRY(ctx);
   const unsigned value = ++ctx->hold_value;
   hold_kernel<<<1, 32, 0, ctx->stream>>>(ctx->hold_dev, value, uint64_t(timeout_us) * 1000ull);
+  GBPOLY_CUDA_TRY(cudaGetLastError());
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_wait_probe(gbpoly_ctx* ctx, uint32_t limit_us) {
+  CTX_TRY(ctx);
+  wait_probe_kernel<<<1, 32, 0, ctx->stream>>>(ctx->err_dev, uint64_t(limit_us) * 1000ull);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
 }

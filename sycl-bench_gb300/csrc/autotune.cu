@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -52,6 +53,23 @@ std::tuple<int, int, int, int> shape_bucket(gbpoly_precision prec, int64_t M, in
 int tuned_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N, int64_t K) {
   auto it = ctx->tuned.find(shape_bucket(prec, M, N, K));
   return it == ctx->tuned.end() ? default_config(ctx, prec, M, N, K) : it->second;
+}
+
+// Problem class of a group: ceil(log2) of the problem count and of the
+// median M, N and K (problems with an empty output excluded).
+std::tuple<int, int, int, int, int> group_class(gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count) {
+  std::vector<int64_t> m, n, k;
+  for(int i = 0; i < count; ++i) {
+    if(descs[i].M <= 0 || descs[i].N <= 0) continue;
+    m.push_back(descs[i].M), n.push_back(descs[i].N), k.push_back(std::max<int64_t>(descs[i].K, 1));
+  }
+  auto median = [](std::vector<int64_t>& v) -> int64_t {
+    if(v.empty()) return 0;
+    std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+    return v[v.size() / 2];
+  };
+  return std::make_tuple(int(prec), ceil_log2(int64_t(m.size())), ceil_log2(median(m)), ceil_log2(median(n)),
+      ceil_log2(median(k)));
 }
 
 }  // namespace gbpoly
@@ -139,6 +157,72 @@ gbpoly_status gbpoly_autotune_gemm(gbpoly_ctx* ctx, gbpoly_precision prec, int64
   return gbpoly_synchronize(ctx);
 }
 
+gbpoly_status gbpoly_grouped_config_count(gbpoly_precision prec, int* count) {
+  if(!count) return fail(GBPOLY_ERR_INVALID, "null output pointer");
+  *count = grouped_config_count(prec);
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_grouped_config_set(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int config) {
+  if(!ctx || count < 0 || (count > 0 && !descs)) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  if(config < 0 || config >= grouped_config_count(prec))
+    return fail(GBPOLY_ERR_INVALID, "no such grouped tile configuration");
+  ctx->tuned_grouped[group_class(prec, descs, count)] = config;
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_grouped_config_get(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int* config) {
+  if(!ctx || !config || count < 0 || (count > 0 && !descs)) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  *config = default_grouped_config(ctx, prec, descs, count);
+  return GBPOLY_OK;
+}
+
+gbpoly_status gbpoly_autotune_grouped(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int reps, int* best_config, float* best_ms) {
+  if(!ctx || count <= 0 || !descs || reps <= 0) return fail(GBPOLY_ERR_INVALID, "bad argument");
+  GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
+  const int nconf = grouped_config_count(prec);
+  if(nconf == 0) return fail(GBPOLY_ERR_UNSUPPORTED, "form has no grouped tile configurations to tune");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if(e == cudaSuccess) e = cudaEventCreate(&e1);
+  if(e != cudaSuccess) {
+    if(e0) cudaEventDestroy(e0);
+    return cuda_fail(e, "autotune events");
+  }
+  gbpoly_status st = GBPOLY_OK;
+  int best = 0;
+  float best_t = INFINITY;
+  for(int c = 0; c < nconf && st == GBPOLY_OK; ++c) {
+    gbpoly_grouped* g = nullptr;
+    if((st = grouped_plan_config(ctx, prec, descs, count, c, &g)) != GBPOLY_OK) break;
+    st = gbpoly_grouped_run(ctx, g);  // warm-up
+    if(st == GBPOLY_OK) {
+      cudaEventRecord(e0, ctx->stream);
+      for(int r = 0; r < reps && st == GBPOLY_OK; ++r) st = gbpoly_grouped_run(ctx, g);
+      cudaEventRecord(e1, ctx->stream);
+      if(st == GBPOLY_OK && (e = cudaEventSynchronize(e1)) != cudaSuccess) st = cuda_fail(e, "autotune timing");
+    }
+    float ms = 0.f;
+    if(st == GBPOLY_OK) cudaEventElapsedTime(&ms, e0, e1);
+    gbpoly_status st2 = gbpoly_grouped_destroy(ctx, g);
+    if(st == GBPOLY_OK) st = st2;
+    if(st == GBPOLY_OK && (st = gbpoly_synchronize(ctx)) == GBPOLY_OK && ms / reps < best_t) {
+      best_t = ms / reps;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if(st != GBPOLY_OK) return st;
+  ctx->tuned_grouped[group_class(prec, descs, count)] = best;
+  if(best_config) *best_config = best;
+  if(best_ms) *best_ms = best_t;
+  return GBPOLY_OK;
+}
+
 gbpoly_status gbpoly_autotune_save(gbpoly_ctx* ctx, const char* path) {
   if(!ctx || !path) return fail(GBPOLY_ERR_INVALID, "bad argument");
   // keep other devices' entries, replace this device's
@@ -156,6 +240,11 @@ gbpoly_status gbpoly_autotune_save(gbpoly_ctx* ctx, const char* path) {
   for(auto& kv : ctx->tuned)
     out << me << "\t" << std::get<0>(kv.first) << "\t" << std::get<1>(kv.first) << "\t" << std::get<2>(kv.first)
         << "\t" << std::get<3>(kv.first) << "\t" << kv.second << "\n";
+  // grouped plans: "G", then form, log2 buckets of count, median M, N, K, configuration
+  for(auto& kv : ctx->tuned_grouped)
+    out << me << "\tG\t" << std::get<0>(kv.first) << "\t" << std::get<1>(kv.first) << "\t"
+        << std::get<2>(kv.first) << "\t" << std::get<3>(kv.first) << "\t" << std::get<4>(kv.first) << "\t"
+        << kv.second << "\n";
   return out.good() ? GBPOLY_OK : fail(GBPOLY_ERR_INVALID, std::string("write failed: ") + path);
 }
 
@@ -168,6 +257,15 @@ gbpoly_status gbpoly_autotune_load(gbpoly_ctx* ctx, const char* path, int* loade
   int n = 0;
   while(std::getline(in, line)) {
     if(line.rfind(me + "\t", 0) != 0) continue;
+    if(line.compare(me.size() + 1, 2, "G\t") == 0) {
+      std::istringstream f(line.substr(me.size() + 3));
+      int prec, cb, bm, bn, bk, config;
+      if(!(f >> prec >> cb >> bm >> bn >> bk >> config)) continue;
+      if(config < 0 || config >= grouped_config_count(gbpoly_precision(prec))) continue;
+      ctx->tuned_grouped[std::make_tuple(prec, cb, bm, bn, bk)] = config;
+      ++n;
+      continue;
+    }
     std::istringstream f(line.substr(me.size() + 1));
     int prec, bm, bn, bk, config;
     if(!(f >> prec >> bm >> bn >> bk >> config)) continue;

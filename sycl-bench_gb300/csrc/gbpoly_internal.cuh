@@ -32,6 +32,7 @@ enum DeviceError : int {
   kDevErrDrainWait = 4,   // teardown waited too long for in-flight copies
   kDevErrTmemAlloc = 5,   // tensor-memory allocation did not fit
   kDevErrSplitWait = 6,   // a K-split tile's first half waited too long for the second
+  kDevErrProbeWait = 7,   // gbpoly_wait_probe: a wait on a barrier nothing completes ran out (as intended)
 };
 
 struct Workspace {
@@ -74,6 +75,9 @@ struct gbpoly_ctx {
   std::vector<cudaEvent_t> event_pool;            // reusable events
   // tile configuration per (form, log2-bucket of M, N, K), from the autotuner
   std::map<std::tuple<int, int, int, int>, int> tuned;
+  // grouped plans: tile configuration per problem class (form, log2-buckets
+  // of the problem count and of the median M, N, K)
+  std::map<std::tuple<int, int, int, int, int>, int> tuned_grouped;
   // host-buffer calls: copy streams and device staging of the operands
   cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
   void *stage_a = nullptr, *stage_b = nullptr, *stage_c = nullptr;
@@ -187,6 +191,14 @@ struct TensorPlan {
 gbpoly_status tensor_plan(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op op_a, gbpoly_op op_b, int64_t M, int64_t N,
     int64_t K, TensorPlan* plan);
 gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const GemmF32Args& a, bool first, int64_t r0);
+// Grouped plans (split_gemm.cu): the number of tile configurations of a form,
+// the problem class a group belongs to (autotune.cu), and planning with a
+// given configuration (-1: the tuned one for the class, else the rule).
+int grouped_config_count(gbpoly_precision prec);
+std::tuple<int, int, int, int, int> group_class(gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count);
+int default_grouped_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count);
+gbpoly_status grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
+    int config, gbpoly_grouped** out);
 // Workspace bytes launch_gemm_tensor needs for this shape (0 for FP32).
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same_operand);
 
@@ -238,9 +250,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Wait for phase `parity` of `bar` to complete.  Returns false (after
-// recording `code` in *err) if it does not within kWaitTimeoutNs, or as soon
-// as another thread of the grid has recorded an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+// recording `code` in *err) if it does not within `limit_ns`, or as soon as
+// another thread of the grid has recorded an error.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, int* err, int code,
+    unsigned long long limit_ns) {
   if(mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_timer_ns();
   while(true) {
@@ -248,11 +261,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
     for(int i = 0; i < 32; ++i)
       if(mbar_try_wait(bar, parity)) return true;
     if(*reinterpret_cast<volatile int*>(err) != 0) return false;
-    if(global_timer_ns() - t0 > kWaitTimeoutNs) {
+    if(global_timer_ns() - t0 > limit_ns) {
       atomicCAS(err, 0, code);
       return false;
     }
   }
+}
+
+// The kernels' waits: mbar_wait_for with the library-wide limit kWaitTimeoutNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  return mbar_wait_for(bar, parity, err, code, kWaitTimeoutNs);
 }
 
 // Wait until the global counter reaches `target` (other CTAs of the same

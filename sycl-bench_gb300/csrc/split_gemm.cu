@@ -192,59 +192,77 @@ struct Term<Elem::TF32> {
 // persistent loop can issue the next block's loads before converting the
 // current one:
 //   split_load:    the block into 16 registers per thread (256 threads),
-//                  coalesced along X's contiguous dimension; 128-bit loads
-//                  when the block is whole and aligned (returns true then);
+//                  coalesced along X's contiguous dimension with 128-bit
+//                  loads: thread t reads elements [4 (t % 16), +4) of the
+//                  block's rows t / 16 + 16 e (e < 4), zero outside R x K;
 //   split_stage:   the registers into the shared tile [r][k];
 //   split_convert: the tile's rows into the term panels.
-__device__ __forceinline__ bool split_load(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
+//
+// Rows that do not start on a 16-byte boundary (a leading dimension that is
+// not a multiple of 4, or an offset base) are read with the aligned 16-byte
+// loads that cover them: a row segment starting a floats (a < 4) past a
+// boundary is read as the chunks at -a and -a + 4 relative to each thread's
+// four elements, and the four are selected from those eight.  Every chunk
+// read holds at least one element of the matrix, so no read leaves the
+// 16-byte granules of the matrix's own elements.
+__device__ __forceinline__ void split_load(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
     int64_t r0, int64_t k0, float (&v)[16]) {
   const int tid = threadIdx.x;
   const int64_t r_lim = R - r0, k_lim = K - k0;
   const int64_t o0 = k_major ? r0 : k0, i0 = k_major ? k0 : r0;  // outer (strided) and inner (contiguous) origin
+  const int out = tid >> 4, q = tid & 15;
   const bool whole = r_lim >= 64 && k_lim >= 64 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
   if(whole) {
-    // float4 e of the thread: outer index tid / 16 + 16 e, inner 4 (tid % 16)
-    const float* p = X + (o0 + (tid >> 4)) * ld + i0 + 4 * (tid & 15);
+    const float* p = X + (o0 + out) * ld + i0 + 4 * q;
 #pragma unroll
     for(int e = 0; e < 4; ++e) {
       const float4 x = *reinterpret_cast<const float4*>(p + e * 16 * ld);
       v[4 * e] = x.x, v[4 * e + 1] = x.y, v[4 * e + 2] = x.z, v[4 * e + 3] = x.w;
     }
-  } else {
-    // element e of the thread: outer index tid / 64 + 4 e, inner tid % 64
-    const int in = tid & 63, out = tid >> 6;
-    const bool in_ok = in < (k_major ? k_lim : r_lim);
-    const int64_t out_lim = k_major ? r_lim : k_lim;
-    const float* p = X + (o0 + out) * ld + i0 + in;
-#pragma unroll
-    for(int e = 0; e < 16; ++e) v[e] = (in_ok && out + 4 * e < out_lim) ? p[e * 4 * ld] : 0.f;
+    return;
   }
-  return whole;
+  const int64_t in_lim = k_major ? k_lim : r_lim, out_lim = k_major ? r_lim : k_lim;
+#pragma unroll
+  for(int e = 0; e < 4; ++e) {
+    const int o = out + 16 * e;
+    float y[4] = {0.f, 0.f, 0.f, 0.f};
+    if(o < out_lim && 4 * q < in_lim) {
+      const float* row = X + (o0 + o) * ld + i0;
+      const int a = int((reinterpret_cast<uintptr_t>(row) >> 2) & 3);
+      const float4* c = reinterpret_cast<const float4*>(row - a) + q;
+      const float4 c0 = c[0];  // holds row[4q]
+      float4 c1 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if(a != 0 && 4 * q + 4 - a < in_lim) c1 = c[1];  // holds row[4q + 4 - a]
+      if(a == 0) {
+        y[0] = c0.x, y[1] = c0.y, y[2] = c0.z, y[3] = c0.w;
+      } else if(a == 1) {
+        y[0] = c0.y, y[1] = c0.z, y[2] = c0.w, y[3] = c1.x;
+      } else if(a == 2) {
+        y[0] = c0.z, y[1] = c0.w, y[2] = c1.x, y[3] = c1.y;
+      } else {
+        y[0] = c0.w, y[1] = c1.x, y[2] = c1.y, y[3] = c1.z;
+      }
+#pragma unroll
+      for(int j = 0; j < 4; ++j)
+        if(4 * q + j >= in_lim) y[j] = 0.f;
+    }
+#pragma unroll
+    for(int j = 0; j < 4; ++j) v[4 * e + j] = y[j];
+  }
 }
 
-__device__ __forceinline__ void split_stage(bool whole, int k_major, const float (&v)[16], float (*tile)[65]) {
+__device__ __forceinline__ void split_stage(int k_major, const float (&v)[16], float (*tile)[65]) {
   const int tid = threadIdx.x;
-  if(whole) {
-    const int out = tid >> 4, in = 4 * (tid & 15);
+  const int out = tid >> 4, in = 4 * (tid & 15);
 #pragma unroll
-    for(int e = 0; e < 4; ++e)
+  for(int e = 0; e < 4; ++e)
 #pragma unroll
-      for(int q = 0; q < 4; ++q) {
-        if(k_major)
-          tile[out + 16 * e][in + q] = v[4 * e + q];
-        else
-          tile[in + q][out + 16 * e] = v[4 * e + q];
-      }
-  } else {
-    const int in = tid & 63, out = tid >> 6;
-#pragma unroll
-    for(int e = 0; e < 16; ++e) {
+    for(int q = 0; q < 4; ++q) {
       if(k_major)
-        tile[out + 4 * e][in] = v[e];
+        tile[out + 16 * e][in + q] = v[4 * e + q];
       else
-        tile[in][out + 4 * e] = v[e];
+        tile[in + q][out + 16 * e] = v[4 * e + q];
     }
-  }
 }
 
 // Terms of 16 consecutive values: t[j] = round(x - t[0] - ... - t[j-1]).
@@ -323,8 +341,8 @@ __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X,
   __shared__ float tile[64][65];
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
   float v[16];
-  const bool whole = split_load(X, ld, k_major, R, K, r0, k0, v);
-  split_stage(whole, k_major, v, tile);
+  split_load(X, ld, k_major, R, K, r0, k0, v);
+  split_stage(k_major, v, tile);
   __syncthreads();
   split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0, xf, K);
 }
@@ -359,10 +377,9 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
   int ji_next = b + step < nblocks ? block_job[b + step] : 0;
   int local = b - j.block_start;
   float v[16];
-  bool whole = split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64,
-      int64_t(local % j.kblocks) * 64, v);
+  split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, v);
   while(true) {
-    split_stage(whole, j.k_major, v, tile);
+    split_stage(j.k_major, v, tile);
     __syncthreads();
     // the current block's job, for its conversion below
     T* const out = static_cast<T*>(j.out);
@@ -374,8 +391,8 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
       j = jobs[ji_next];
       ji_next = nb + step < nblocks ? block_job[nb + step] : 0;
       local = nb - j.block_start;
-      whole = split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64,
-          int64_t(local % j.kblocks) * 64, v);
+      split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64,
+          v);
     }
     split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0);
     if(nb >= nblocks) break;
@@ -1527,7 +1544,7 @@ struct gbpoly_grouped {
   int* block_job = nullptr;  // split block -> job
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
-  bool pairs = false;  // CTA-pair (256 x 256) tiles instead of 128 x 128
+  int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3) 128 x 256
 };
 
 namespace gbpoly {
@@ -1633,11 +1650,14 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
   return launch_tc_kernel<F>(ctx, sched, g->ntiles, name);
 }
 
-// Grouped calls use the 128-column tile configurations (less padding on
-// small problems), or the CTA-pair configurations when every problem is
-// large enough that 256 x 256 tiles pad it about as little and the group
-// fills at least two rounds of pairs (a few large products, as matmulchain's
-// two independent stages).
+// Tile configurations of grouped plans: 0 = 1-CTA 128 x 128 tiles (least
+// padding of small problems), 1 = CTA pairs on 256 x 256 tiles (a few large
+// products, as matmulchain's two independent stages), and for bf16x3 2 =
+// 1-CTA 128 x 256 tiles.  Untuned, a group uses 1 when every problem is
+// large enough that 256 x 256 tiles pad it about as little as 128 x 128 ones
+// and the group fills at least two rounds of pairs, else 0; the autotuner
+// (gbpoly_autotune_grouped) times them per problem class.
+using GroupBF16x3_w = FormBF16x3;
 using GroupBF16x3 = FormBF16x3_c;
 using GroupTF32x3 = FormTF32x3_c;
 using GroupBF16x6 = FormBF16x6_b;
@@ -1661,12 +1681,37 @@ bool grouped_pairs(gbpoly_ctx* ctx, const std::vector<gbpoly_gemm_desc>& descs) 
 }
 
 }  // namespace
+
+int grouped_config_count(gbpoly_precision prec) {
+  switch(prec) {
+  case GBPOLY_PREC_BF16X3: return 3;
+  case GBPOLY_PREC_TF32X3:
+  case GBPOLY_PREC_BF16X6:
+  case GBPOLY_PREC_TF32: return 2;
+  default: return 0;
+  }
+}
+
+int default_grouped_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count) {
+  if(grouped_config_count(prec) == 0) return 0;
+  auto it = ctx->tuned_grouped.find(group_class(prec, descs, count));
+  if(it != ctx->tuned_grouped.end() && it->second < grouped_config_count(prec)) return it->second;
+  return grouped_pairs(ctx, std::vector<gbpoly_gemm_desc>(descs, descs + count)) ? 1 : 0;
+}
+
 }  // namespace gbpoly
 
 extern "C" {
 
 gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
     gbpoly_grouped** out) {
+  return gbpoly::grouped_plan_config(ctx, prec, descs, count, -1, out);
+}
+
+}  // extern "C"
+
+gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs,
+    int count, int config, gbpoly_grouped** out) {
   using namespace gbpoly;
   if(!ctx || !out || count < 0 || (count > 0 && !descs)) return fail(GBPOLY_ERR_INVALID, "bad argument");
   *out = nullptr;
@@ -1711,15 +1756,20 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6:
   case GBPOLY_PREC_TF32:
-    g->pairs = grouped_pairs(ctx, g->descs);
-    switch(prec * 2 + (g->pairs ? 1 : 0)) {
-    case GBPOLY_PREC_BF16X3 * 2: st = plan_grouped<GroupBF16x3>(ctx, g); break;
-    case GBPOLY_PREC_BF16X3 * 2 + 1: st = plan_grouped<GroupBF16x3_p>(ctx, g); break;
-    case GBPOLY_PREC_TF32X3 * 2: st = plan_grouped<GroupTF32x3>(ctx, g); break;
-    case GBPOLY_PREC_TF32X3 * 2 + 1: st = plan_grouped<GroupTF32x3_p>(ctx, g); break;
-    case GBPOLY_PREC_BF16X6 * 2: st = plan_grouped<GroupBF16x6>(ctx, g); break;
-    case GBPOLY_PREC_BF16X6 * 2 + 1: st = plan_grouped<GroupBF16x6_p>(ctx, g); break;
-    case GBPOLY_PREC_TF32 * 2: st = plan_grouped<GroupTF32>(ctx, g); break;
+    g->config = config >= 0 ? config : default_grouped_config(ctx, prec, descs, count);
+    if(g->config >= grouped_config_count(prec)) {
+      st = fail(GBPOLY_ERR_INVALID, "no such grouped tile configuration");
+      break;
+    }
+    switch(prec * 4 + g->config) {
+    case GBPOLY_PREC_BF16X3 * 4: st = plan_grouped<GroupBF16x3>(ctx, g); break;
+    case GBPOLY_PREC_BF16X3 * 4 + 1: st = plan_grouped<GroupBF16x3_p>(ctx, g); break;
+    case GBPOLY_PREC_BF16X3 * 4 + 2: st = plan_grouped<GroupBF16x3_w>(ctx, g); break;
+    case GBPOLY_PREC_TF32X3 * 4: st = plan_grouped<GroupTF32x3>(ctx, g); break;
+    case GBPOLY_PREC_TF32X3 * 4 + 1: st = plan_grouped<GroupTF32x3_p>(ctx, g); break;
+    case GBPOLY_PREC_BF16X6 * 4: st = plan_grouped<GroupBF16x6>(ctx, g); break;
+    case GBPOLY_PREC_BF16X6 * 4 + 1: st = plan_grouped<GroupBF16x6_p>(ctx, g); break;
+    case GBPOLY_PREC_TF32 * 4: st = plan_grouped<GroupTF32>(ctx, g); break;
     default: st = plan_grouped<GroupTF32_p>(ctx, g); break;
     }
     break;
@@ -1733,6 +1783,8 @@ gbpoly_status gbpoly_grouped_plan(gbpoly_ctx* ctx, gbpoly_precision prec, const 
   *out = g;
   return GBPOLY_OK;
 }
+
+extern "C" {
 
 gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   using namespace gbpoly;
@@ -1750,19 +1802,26 @@ gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
     }
     return GBPOLY_OK;
   case GBPOLY_PREC_BF16X3:
-    return g->pairs ? run_grouped<GroupBF16x3_p>(ctx, g, "grouped_bf16x3_gemm")
-                    : run_grouped<GroupBF16x3>(ctx, g, "grouped_bf16x3_gemm");
+    return g->config == 1   ? run_grouped<GroupBF16x3_p>(ctx, g, "grouped_bf16x3_gemm")
+           : g->config == 2 ? run_grouped<GroupBF16x3_w>(ctx, g, "grouped_bf16x3_gemm")
+                            : run_grouped<GroupBF16x3>(ctx, g, "grouped_bf16x3_gemm");
   case GBPOLY_PREC_TF32X3:
-    return g->pairs ? run_grouped<GroupTF32x3_p>(ctx, g, "grouped_tf32x3_gemm")
-                    : run_grouped<GroupTF32x3>(ctx, g, "grouped_tf32x3_gemm");
+    return g->config == 1 ? run_grouped<GroupTF32x3_p>(ctx, g, "grouped_tf32x3_gemm")
+                          : run_grouped<GroupTF32x3>(ctx, g, "grouped_tf32x3_gemm");
   case GBPOLY_PREC_BF16X6:
-    return g->pairs ? run_grouped<GroupBF16x6_p>(ctx, g, "grouped_bf16x6_gemm")
-                    : run_grouped<GroupBF16x6>(ctx, g, "grouped_bf16x6_gemm");
+    return g->config == 1 ? run_grouped<GroupBF16x6_p>(ctx, g, "grouped_bf16x6_gemm")
+                          : run_grouped<GroupBF16x6>(ctx, g, "grouped_bf16x6_gemm");
   case GBPOLY_PREC_TF32:
-    return g->pairs ? run_grouped<GroupTF32_p>(ctx, g, "grouped_tf32_gemm")
-                    : run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
+    return g->config == 1 ? run_grouped<GroupTF32_p>(ctx, g, "grouped_tf32_gemm")
+                          : run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   }
+}
+
+gbpoly_status gbpoly_grouped_config_of(gbpoly_grouped* g, int* config) {
+  if(!g || !config) return gbpoly::fail(GBPOLY_ERR_INVALID, "bad argument");
+  *config = g->config;
+  return GBPOLY_OK;
 }
 
 gbpoly_status gbpoly_grouped_info(gbpoly_grouped* g, int64_t* flops, int* tiles, size_t* device_bytes) {

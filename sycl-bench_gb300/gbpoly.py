@@ -117,6 +117,7 @@ SIGNATURES: dict[str, tuple] = {
                                     ct.c_float, _vp, _c_i64]),
     "gbpoly_stream_hold": (ct.c_int, [_vp, ct.c_uint32]),
     "gbpoly_stream_release": (ct.c_int, [_vp]),
+    "gbpoly_wait_probe": (ct.c_int, [_vp, ct.c_uint32]),
     "gbpoly_gemv_f32": (ct.c_int, [_vp, ct.c_int, _c_i64, _c_i64, ct.c_float, _vp, _c_i64, _vp, ct.c_float, _vp]),
     "gbpoly_atax_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, _vp, _vp]),
     "gbpoly_gemv_pair_f32": (ct.c_int, [_vp, _c_i64, _c_i64, _vp, _c_i64, _vp, ct.c_int]),
@@ -133,6 +134,12 @@ SIGNATURES: dict[str, tuple] = {
     "gbpoly_grouped_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int), ct.POINTER(ct.c_size_t)]),
     "gbpoly_grouped_destroy": (ct.c_int, [_vp, _vp]),
     "gbpoly_gemm_grouped_f32": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int]),
+    "gbpoly_grouped_config_of": (ct.c_int, [_vp, ct.POINTER(ct.c_int)]),
+    "gbpoly_grouped_config_count": (ct.c_int, [ct.c_int, ct.POINTER(ct.c_int)]),
+    "gbpoly_grouped_config_set": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.c_int]),
+    "gbpoly_grouped_config_get": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.POINTER(ct.c_int)]),
+    "gbpoly_autotune_grouped": (ct.c_int, [_vp, ct.c_int, _vp, ct.c_int, ct.c_int, ct.POINTER(ct.c_int),
+                                           ct.POINTER(ct.c_float)]),
     "gbpoly_gemm_f32_bf16x3_noalloc": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_float, _vp,
                                                   _c_i64, _vp, _c_i64, ct.c_float, _vp, _c_i64]),
     "gbpoly_gemm_f64": (ct.c_int, [_vp, ct.c_int, ct.c_int, _c_i64, _c_i64, _c_i64, ct.c_double, _vp, _c_i64, _vp,
@@ -378,6 +385,32 @@ class Context:
         _check(self.lib.gbpoly_grouped_info(plan, ct.byref(f), ct.byref(t), ct.byref(b)))
         return {"flops": f.value, "tiles": t.value, "device_bytes": b.value}
 
+    def grouped_config_of(self, plan) -> int:
+        c = ct.c_int()
+        _check(self.lib.gbpoly_grouped_config_of(plan, ct.byref(c)))
+        return c.value
+
+    def grouped_config_count(self, prec) -> int:
+        c = ct.c_int()
+        _check(self.lib.gbpoly_grouped_config_count(int(prec), ct.byref(c)))
+        return c.value
+
+    def grouped_config_set(self, prec, descs, config: int) -> None:
+        _check(self.lib.gbpoly_grouped_config_set(self.handle, int(prec), ct.cast(descs, _vp), len(descs), config))
+
+    def grouped_config_get(self, prec, descs) -> int:
+        c = ct.c_int()
+        _check(self.lib.gbpoly_grouped_config_get(self.handle, int(prec), ct.cast(descs, _vp), len(descs),
+                                                  ct.byref(c)))
+        return c.value
+
+    def autotune_grouped(self, prec, descs, reps: int = 3) -> tuple[int, float]:
+        """Time every grouped tile configuration on these problems (C is overwritten); keep the fastest."""
+        c, ms = ct.c_int(), ct.c_float()
+        _check(self.lib.gbpoly_autotune_grouped(self.handle, int(prec), ct.cast(descs, _vp), len(descs), reps,
+                                                ct.byref(c), ct.byref(ms)))
+        return c.value, ms.value
+
     def grouped_destroy(self, plan) -> None:
         _check(self.lib.gbpoly_grouped_destroy(self.handle, plan))
 
@@ -421,6 +454,10 @@ class Context:
 
     def stream_release(self) -> None:
         _check(self.lib.gbpoly_stream_release(self.handle))
+
+    def wait_probe(self, limit_us: int) -> None:
+        """Queue a bounded wait that runs out after limit_us (the next synchronize reports TIMEOUT)."""
+        _check(self.lib.gbpoly_wait_probe(self.handle, limit_us))
 
     # -- matrix-vector products (atax, bicg, mvt, gesummv)
     def gemv(self, op, rows, cols, alpha, A, lda, x, beta, y) -> None:

@@ -149,3 +149,69 @@ def test_grouped_large_problems_run_on_cta_pairs(ctx, prec):
     for b in bufs:
         for x in b:
             ctx.free(x)
+
+
+def group_descs(ctx, probs):
+    items, bufs = [], []
+    for op_a, op_b, M, N, K, A, B, C in probs:
+        dA = ctx.upload(A) if A.size else ctx.alloc(16)
+        dB = ctx.upload(B) if B.size else ctx.alloc(16)
+        dC = ctx.upload(C)
+        bufs.append((dA, dB, dC))
+        items.append(dict(op_a=op_a, op_b=op_b, M=M, N=N, K=K, alpha=1.0, beta=0.5, A=dA, lda=max(A.shape[1], 1),
+                          B=dB, ldb=max(B.shape[1], 1), C=dC, ldc=N))
+    return ctx.descs(items), bufs
+
+
+@pytest.mark.parametrize("prec", list(BOUND))
+def test_every_grouped_configuration_is_correct(ctx, prec):
+    """Each grouped tile configuration (forced per problem class) matches FP64 per problem."""
+    rng = np.random.default_rng(33)
+    probs = make_problems(rng, 20, 40, 600)
+    descs, bufs = group_descs(ctx, probs)
+    for cfg in range(ctx.grouped_config_count(prec)):
+        ctx.grouped_config_set(prec, descs, cfg)
+        assert ctx.grouped_config_get(prec, descs) == cfg
+        for (_, _, _, _, _, _, _, C), (_, _, dC) in zip(probs, bufs):
+            ctx.h2d(dC, C)
+        plan = ctx.grouped_plan(prec, descs)
+        assert ctx.grouped_config_of(plan) == cfg
+        ctx.grouped_run(plan)
+        ctx.synchronize()
+        for (op_a, op_b, M, N, K, A, B, C), (_, _, dC) in zip(probs, bufs):
+            out = ctx.download(dC, (M, N))
+            ref = oracle.gemm_f64(A, B, C, 1.0, 0.5, op_a=int(op_a), op_b=int(op_b)) if K else 0.5 * C.astype(
+                np.float64)
+            assert oracle.error_norms(out, ref)[1] < BOUND[prec], (cfg, M, N, K)
+        ctx.grouped_destroy(plan)
+    for b in bufs:
+        for x in b:
+            ctx.free(x)
+
+
+def test_grouped_autotune_records_and_persists(ctx, tmp_path):
+    """The grouped autotuner times every configuration on the group, keeps the
+    fastest for the group's class (the next plan of that class uses it), and
+    the entry survives save / load into a new context."""
+    import gbpoly
+    prec = Precision.BF16X3
+    rng = np.random.default_rng(34)
+    probs = make_problems(rng, 24, 64, 900)
+    descs, bufs = group_descs(ctx, probs)
+    best, ms = ctx.autotune_grouped(prec, descs, reps=2)
+    assert 0 <= best < ctx.grouped_config_count(prec) and ms > 0
+    assert ctx.grouped_config_get(prec, descs) == best
+    plan = ctx.grouped_plan(prec, descs)
+    assert ctx.grouped_config_of(plan) == best
+    ctx.grouped_destroy(plan)
+    other = (best + 1) % ctx.grouped_config_count(prec)
+    ctx.grouped_config_set(prec, descs, other)
+    path = tmp_path / "tuned.txt"
+    ctx.autotune_save(path)
+    assert "\tG\t" in path.read_text()
+    with gbpoly.Context(0) as fresh:
+        assert fresh.autotune_load(path) >= 1
+        assert fresh.grouped_config_get(prec, descs) == other
+    for b in bufs:
+        for x in b:
+            ctx.free(x)
