@@ -972,6 +972,9 @@ def run_grouped_workload(ctx, args) -> dict:
     descs = ctx.descs(items)
     for prec, mode in ((Precision.FP32, "per-GEMM launches"), (Precision.BF16X3, "grouped plan in a CUDA graph"),
                        (Precision.BF16X6, "grouped plan in a CUDA graph")):
+        tuned = None
+        if prec != Precision.FP32:  # the grouped autotuner picks the tile configuration for this problem class
+            tuned = ctx.autotune_grouped(prec, descs, reps=3)
         plan = ctx.grouped_plan(prec, descs)
         reset_c()
         ctx.grouped_run(plan)
@@ -1009,6 +1012,9 @@ def run_grouped_workload(ctx, args) -> dict:
                                   "launches_per_step": 2 if graph is not None else count,
                                   "kernel_ms_eager": kern if graph is not None else
                                   {"sgemm (all launches)": round(sum(kern.values()), 4)}}
+        if tuned is not None:
+            out[prec.name.lower()]["tile_config"] = ctx.grouped_config_of(plan)
+            out[prec.name.lower()]["autotune_best_ms"] = tuned[1]
         if graph is not None:
             ctx.graph_destroy(graph)
         ctx.grouped_destroy(plan)
@@ -1024,6 +1030,8 @@ def run_grouped_workload(ctx, args) -> dict:
              "bytes": "sum of 4 (M K + K N + 2 M N): A, B read, C read and written"}
     sub_descs = ctx.descs([items[i] for i in sub])
     for prec in (Precision.FP32, Precision.BF16X3):
+        if prec != Precision.FP32:
+            ctx.autotune_grouped(prec, sub_descs, reps=3)
         plan = ctx.grouped_plan(prec, sub_descs)
         graph = None
         if prec != Precision.FP32:
@@ -1048,6 +1056,8 @@ def run_grouped_workload(ctx, args) -> dict:
         ms = e0.elapsed_ms(e1) / args.steps
         gbs = sub_bytes / (ms * 1e-3) / 1e9
         small[prec.name.lower()] = {"ms_per_step": ms, "gbs": gbs, "frac_of_hbm": gbs / hbm if hbm else None}
+        if prec != Precision.FP32:
+            small[prec.name.lower()]["tile_config"] = ctx.grouped_config_of(plan)
         if graph is not None:
             ctx.graph_destroy(graph)
         ctx.grouped_destroy(plan)

@@ -188,21 +188,30 @@ struct Term<Elem::TF32> {
 };
 
 // ------------------------------------------------------------- split pass --
-// One 64 x 64 block of op(X) at (r0, k0) in three steps, so that a
-// persistent loop can issue the next block's loads before converting the
-// current one:
-//   split_load:    the block into 16 registers per thread (256 threads),
-//                  coalesced along X's contiguous dimension with 128-bit
-//                  loads: thread t reads elements [4 (t % 16), +4) of the
-//                  block's rows t / 16 + 16 e (e < 4), zero outside R x K;
-//   split_stage:   the registers into the shared tile [r][k];
-//   split_convert: the tile's rows into the term panels.
+// One 64 x 64 block of op(X) at (r0, k0) per CTA of 256 threads (or per
+// iteration of a persistent CTA), without a shared-memory tile: every thread
+// converts 16 values it loaded itself, coalesced in both layouts.
+//   K-major op(X) (op(X)[r][k] = X[r ld + k], rows contiguous in k):
+//     split_load gives thread t elements [4 (t % 16), +4) of the block's rows
+//     t / 16 + 16 e (e < 4), with 16-byte loads; split_convert_kmajor writes
+//     their terms (8 bytes of BF16 or 16 of TF32 per row and term).
+//   MN-major op(X) (op(X)[r][k] = X[k ld + r]): warp w holds block rows
+//     r = 32 (w % 2) + lane and k in [16 (w / 2), +16); each of its 16 loads
+//     is one 128-byte segment of a row of X across the warp, and the 16
+//     values a lane holds are 16 consecutive k of output row r: the
+//     transposition is the register assignment itself.  split_convert_mn
+//     writes the row's terms (32 bytes of BF16 or 64 of TF32 per term).
+// Values outside R x K are zero, so the K padding of the panels is written
+// with zeros.  Both convert the same way: terms by SplitTerms, an optional
+// per-row transform first (RowXform).
 //
-// Rows that do not start on a 16-byte boundary (a leading dimension that is
-// not a multiple of 4, or an offset base) are read with the aligned 16-byte
-// loads that cover them: a row segment starting a floats (a < 4) past a
-// boundary is read as the chunks at -a and -a + 4 relative to each thread's
-// four elements, and the four are selected from those eight.  Every chunk
+// Rows of a K-major operand that do not start on a 16-byte boundary (a
+// leading dimension that is not a multiple of 4, or an offset base) are read
+// with the aligned 16-byte loads that cover them: a row segment starting a
+// floats (a < 4) past a boundary is covered by 17 chunks; lane q of a half
+// warp (one row) loads chunk q, takes chunk q + 1 from its neighbour by a
+// shuffle (lane 15 loads chunk 16 itself), and selects its four elements
+// with two branch-free shift stages (by a & 1, then by a & 2).  Every chunk
 // read holds at least one element of the matrix, so no read leaves the
 // 16-byte granules of the matrix's own elements.
 __device__ __forceinline__ void split_load(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
@@ -222,58 +231,58 @@ __device__ __forceinline__ void split_load(const float* __restrict__ X, int64_t 
     return;
   }
   const int64_t in_lim = k_major ? k_lim : r_lim, out_lim = k_major ? r_lim : k_lim;
+  float4 c[4], x16[4];
+  int al[4];
+#pragma unroll
+  for(int e = 0; e < 4; ++e) {  // all loads first
+    const int o = out + 16 * e;
+    const bool row_ok = o < out_lim;
+    const float* row = X + (o0 + (row_ok ? o : 0)) * ld + i0;
+    const int a = int((reinterpret_cast<uintptr_t>(row) >> 2) & 3);
+    const float4* ch = reinterpret_cast<const float4*>(row - a);
+    al[e] = a;
+    c[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    x16[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if(row_ok && max(4 * q - a, 0) < in_lim) c[e] = ch[q];          // holds row[max(4q - a, 0)]
+    if(row_ok && q == 15 && a != 0 && 64 - a < in_lim) x16[e] = ch[16];  // holds row[64 - a]
+  }
 #pragma unroll
   for(int e = 0; e < 4; ++e) {
-    const int o = out + 16 * e;
-    float y[4] = {0.f, 0.f, 0.f, 0.f};
-    if(o < out_lim && 4 * q < in_lim) {
-      const float* row = X + (o0 + o) * ld + i0;
-      const int a = int((reinterpret_cast<uintptr_t>(row) >> 2) & 3);
-      const float4* c = reinterpret_cast<const float4*>(row - a) + q;
-      const float4 c0 = c[0];  // holds row[4q]
-      float4 c1 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if(a != 0 && 4 * q + 4 - a < in_lim) c1 = c[1];  // holds row[4q + 4 - a]
-      if(a == 0) {
-        y[0] = c0.x, y[1] = c0.y, y[2] = c0.z, y[3] = c0.w;
-      } else if(a == 1) {
-        y[0] = c0.y, y[1] = c0.z, y[2] = c0.w, y[3] = c1.x;
-      } else if(a == 2) {
-        y[0] = c0.z, y[1] = c0.w, y[2] = c1.x, y[3] = c1.y;
-      } else {
-        y[0] = c0.w, y[1] = c1.x, y[2] = c1.y, y[3] = c1.z;
-      }
+    float4 n;
+    n.x = __shfl_down_sync(0xffffffffu, c[e].x, 1, 16);
+    n.y = __shfl_down_sync(0xffffffffu, c[e].y, 1, 16);
+    n.z = __shfl_down_sync(0xffffffffu, c[e].z, 1, 16);
+    if(q == 15) n = x16[e];
+    const int a = al[e];
+    // w = c0.x c0.y c0.z c0.w n.x n.y n.z; element j of the thread is w[j + a]
+    const bool s1 = a & 1, s2 = a & 2;
+    const float u0 = s1 ? c[e].y : c[e].x, u1 = s1 ? c[e].z : c[e].y, u2 = s1 ? c[e].w : c[e].z;
+    const float u3 = s1 ? n.x : c[e].w, u4 = s1 ? n.y : n.x, u5 = s1 ? n.z : n.y;
+    float y[4] = {s2 ? u2 : u0, s2 ? u3 : u1, s2 ? u4 : u2, s2 ? u5 : u3};
+    const bool row_ok = out + 16 * e < out_lim;
 #pragma unroll
-      for(int j = 0; j < 4; ++j)
-        if(4 * q + j >= in_lim) y[j] = 0.f;
-    }
-#pragma unroll
-    for(int j = 0; j < 4; ++j) v[4 * e + j] = y[j];
+    for(int j = 0; j < 4; ++j) v[4 * e + j] = (row_ok && 4 * q + j < in_lim) ? y[j] : 0.f;
   }
 }
 
-__device__ __forceinline__ void split_stage(int k_major, const float (&v)[16], float (*tile)[65]) {
-  const int tid = threadIdx.x;
-  const int out = tid >> 4, in = 4 * (tid & 15);
+__device__ __forceinline__ void split_load_mn(const float* __restrict__ X, int64_t ld, int R, int K, int64_t r0,
+    int64_t k0, float (&v)[16]) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = r0 + 32 * (warp & 1) + lane, k = k0 + 16 * (warp >> 1);
+  const float* p = X + k * ld + r;
 #pragma unroll
-  for(int e = 0; e < 4; ++e)
-#pragma unroll
-    for(int q = 0; q < 4; ++q) {
-      if(k_major)
-        tile[out + 16 * e][in + q] = v[4 * e + q];
-      else
-        tile[in + q][out + 16 * e] = v[4 * e + q];
-    }
+  for(int i = 0; i < 16; ++i) v[i] = (r < R && k + i < K) ? p[int64_t(i) * ld] : 0.f;
 }
 
-// Terms of 16 consecutive values: t[j] = round(x - t[0] - ... - t[j-1]).
+// Terms of NV consecutive values: t[j] = round(x - t[0] - ... - t[j-1]).
 // BF16: two values per conversion (cvt.rn.bf16x2.f32, the same round to
 // nearest even as one at a time).
-template <Elem E, int TERMS>
+template <Elem E, int TERMS, int NV = 16>
 struct SplitTerms {
   using T = typename Term<E>::T;
-  __device__ static void run(const float* x, T (&t)[TERMS][16]) {
+  __device__ static void run(const float* x, T (&t)[TERMS][NV]) {
 #pragma unroll
-    for(int i = 0; i < 16; ++i) {
+    for(int i = 0; i < NV; ++i) {
       float rem = x[i];
 #pragma unroll
       for(int j = 0; j < TERMS; ++j) {
@@ -283,11 +292,11 @@ struct SplitTerms {
     }
   }
 };
-template <int TERMS>
-struct SplitTerms<Elem::BF16, TERMS> {
-  __device__ static void run(const float* x, __nv_bfloat16 (&t)[TERMS][16]) {
+template <int TERMS, int NV>
+struct SplitTerms<Elem::BF16, TERMS, NV> {
+  __device__ static void run(const float* x, __nv_bfloat16 (&t)[TERMS][NV]) {
 #pragma unroll
-    for(int i = 0; i < 16; i += 2) {
+    for(int i = 0; i < NV; i += 2) {
       float a = x[i], b = x[i + 1];
 #pragma unroll
       for(int j = 0; j < TERMS; ++j) {
@@ -301,24 +310,60 @@ struct SplitTerms<Elem::BF16, TERMS> {
   }
 };
 
+// K-major operands (op(X) rows contiguous in X) need no transposition: each
+// thread converts the values split_load gave it (rows t / 16 + 16 e, k
+// elements [4 (t % 16), +4)) straight into the panels, the same arithmetic as
+// split_convert (row transform included), without the shared tile.
 template <Elem E, int TERMS>
-__device__ __forceinline__ void split_convert(const float (*tile)[65], typename Term<E>::T* __restrict__ out,
+__device__ __forceinline__ void split_convert_kmajor(const float (&v)[16], typename Term<E>::T* __restrict__ out,
     int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0, RowXform xf = RowXform{}, int K = 0) {
   using T = typename Term<E>::T;
   const int tid = threadIdx.x;
-  const int rr = tid >> 2, kc = (tid & 3) * 16;
-  const int64_t r = r0 + rr;
+  const int rr = tid >> 4, kc = 4 * (tid & 15);
+#pragma unroll
+  for(int e = 0; e < 4; ++e) {
+    const int64_t r = r0 + rr + 16 * e;
+    if(r >= R) continue;
+    float x[4] = {v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]};
+    if(xf.mean) {
+      const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
+#pragma unroll
+      for(int i = 0; i < 4; ++i) {
+        float y = x[i] - m;
+        if(xf.sd) y = (y / xf.div) / sd;
+        x[i] = k0 + kc + i < K ? y : 0.f;
+      }
+    }
+    __align__(16) T t[TERMS][4];
+    SplitTerms<E, TERMS, 4>::run(x, t);
+#pragma unroll
+    for(int j = 0; j < TERMS; ++j) {
+      T* dst = out + j * panel_stride + r * Kp + k0 + kc;
+      if constexpr(sizeof(T) == 2)
+        *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(t[j]);
+      else
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(t[j]);
+    }
+  }
+}
+
+template <Elem E, int TERMS>
+__device__ __forceinline__ void split_convert_mn(const float (&v)[16], typename Term<E>::T* __restrict__ out,
+    int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0, RowXform xf = RowXform{}, int K = 0) {
+  using T = typename Term<E>::T;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = r0 + 32 * (warp & 1) + lane, kc = k0 + 16 * (warp >> 1);
   if(r >= R) return;
   float x[16];
 #pragma unroll
-  for(int i = 0; i < 16; ++i) x[i] = tile[rr][kc + i];
+  for(int i = 0; i < 16; ++i) x[i] = v[i];
   if(xf.mean) {  // the row's transform, on the elements inside K (the K padding stays zero)
     const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
 #pragma unroll
     for(int i = 0; i < 16; ++i) {
       float y = x[i] - m;
       if(xf.sd) y = (y / xf.div) / sd;
-      x[i] = k0 + kc + i < K ? y : 0.f;
+      x[i] = kc + i < K ? y : 0.f;
     }
   }
   __align__(16) T t[TERMS][16];
@@ -326,9 +371,9 @@ __device__ __forceinline__ void split_convert(const float (*tile)[65], typename 
   constexpr int kVec = 16 * sizeof(T) / 16;  // uint4 per 16 elements
 #pragma unroll
   for(int j = 0; j < TERMS; ++j) {
-    uint4* dst = reinterpret_cast<uint4*>(out + j * panel_stride + r * Kp + k0 + kc);
+    uint4* dst = reinterpret_cast<uint4*>(out + j * panel_stride + r * Kp + kc);
 #pragma unroll
-    for(int v = 0; v < kVec; ++v) dst[v] = reinterpret_cast<const uint4*>(t[j])[v];
+    for(int w = 0; w < kVec; ++w) dst[w] = reinterpret_cast<const uint4*>(t[j])[w];
   }
 }
 
@@ -338,147 +383,146 @@ __device__ __forceinline__ void split_convert(const float (*tile)[65], typename 
 template <Elem E, int TERMS>
 __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
     int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride, RowXform xf) {
-  __shared__ float tile[64][65];
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
   float v[16];
-  split_load(X, ld, k_major, R, K, r0, k0, v);
-  split_stage(k_major, v, tile);
-  __syncthreads();
-  split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0, xf, K);
+  if(k_major) {
+    split_load(X, ld, k_major, R, K, r0, k0, v);
+    split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
+  } else {
+    split_load_mn(X, ld, R, K, r0, k0, v);
+    split_convert_mn<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
+  }
 }
 
-// One operand of a grouped call: its 64x64 blocks are blocks
-// [block_start, block_start + ceil(R/64) * Kp/64) of the grouped split pass,
-// row block by row block.
+// One operand of a grouped call; its 64 x 64 blocks are listed in the
+// plan's block table.
 struct SplitJob {
   const float* X;
   int64_t ld;
   int k_major, R, K, Kp;
   void* out;
   int64_t panel_stride;  // elements
-  int block_start, kblocks;
 };
 
 // Grouped split pass: persistent CTAs walk the blocks in a grid-stride loop
 // (block b, b + gridDim.x, ...: the blocks in flight at a time are
-// neighbours in memory, as in a one-block-per-CTA launch), loading the next
-// block while converting the current one.  block_job[b] (written by the
-// plan) gives a block's job; the job index of the block after next is read
-// one iteration ahead.
+// neighbours in memory, as in a one-block-per-CTA launch); blocks[b] =
+// (job, row block, k block) is written by the plan.  The load latency is
+// covered by the 32 resident warps per SM, each with 16 loads in flight.
 template <Elem E, int TERMS>
 __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* __restrict__ jobs,
-    const int* __restrict__ block_job, int nblocks) {
+    const int4* __restrict__ blocks, int nblocks) {
   using T = typename Term<E>::T;
-  __shared__ float tile[64][65];
-  const int step = gridDim.x;
-  int b = blockIdx.x;
-  if(b >= nblocks) return;
-  SplitJob j = jobs[block_job[b]];
-  int ji_next = b + step < nblocks ? block_job[b + step] : 0;
-  int local = b - j.block_start;
-  float v[16];
-  split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64, v);
-  while(true) {
-    split_stage(j.k_major, v, tile);
-    __syncthreads();
-    // the current block's job, for its conversion below
-    T* const out = static_cast<T*>(j.out);
-    const int64_t panel_stride = j.panel_stride, r0 = int64_t(local / j.kblocks) * 64,
-                  k0 = int64_t(local % j.kblocks) * 64;
-    const int R = j.R, Kp = j.Kp;
-    const int nb = b + step;
-    if(nb < nblocks) {  // next block's loads in flight during the conversion
-      j = jobs[ji_next];
-      ji_next = nb + step < nblocks ? block_job[nb + step] : 0;
-      local = nb - j.block_start;
-      split_load(j.X, j.ld, j.k_major, j.R, j.K, int64_t(local / j.kblocks) * 64, int64_t(local % j.kblocks) * 64,
-          v);
+  for(int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    const int4 bl = blocks[b];
+    const SplitJob j = jobs[bl.x];
+    const int64_t r0 = int64_t(bl.y) * 64, k0 = int64_t(bl.z) * 64;
+    float v[16];
+    if(j.k_major) {
+      split_load(j.X, j.ld, 1, j.R, j.K, r0, k0, v);
+      split_convert_kmajor<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
+    } else {
+      split_load_mn(j.X, j.ld, j.R, j.K, r0, k0, v);
+      split_convert_mn<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
     }
-    split_convert<E, TERMS>(tile, out, panel_stride, R, Kp, r0, k0);
-    if(nb >= nblocks) break;
-    b = nb;
-    __syncthreads();  // the tile is read before the next block overwrites it
   }
 }
 
 // ---------------------------------------------------------- FP8 quantize --
-// One 128 x 128 block of op(X) (rows x K, zero beyond R and K) per CTA:
-// scale = max|x| / 448 (1 for an all-zero block), q = e4m3(x / scale) with
-// saturation, written K-major into out[R][Kp]; scale into
-// scales[row block][Kp / 128].
-__global__ void __launch_bounds__(256) quantize_e4m3_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R,
-    int K, int Kp, uint8_t* __restrict__ out, float* __restrict__ scales) {
-  extern __shared__ float blk[];  // [128][129]
-  __shared__ float red[8];
-  const int tid = threadIdx.x;
-  const int64_t r0 = int64_t(blockIdx.y) * 128, k0 = int64_t(blockIdx.x) * 128;
-  const int64_t o0 = k_major ? r0 : k0, i0 = k_major ? k0 : r0;  // outer (strided) and inner (contiguous) origin
-  const bool whole = R - r0 >= 128 && K - k0 >= 128 && (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
-  float amax = 0.f;
-  if(whole) {
-    // float4 e of the thread: outer index tid / 32 + 8 e, inner 4 (tid % 32);
-    // all 16 loads in flight before the shared-memory stores
-    const int out = tid >> 5, in = 4 * (tid & 31);
-    const float* p = X + (o0 + out) * ld + i0 + in;
-    float4 v[16];
+// 128 x 128 blocks of op(X) (rows x K, zero beyond R and K), one per CTA of
+// 512 threads: scale = max|x| / 448 (1 for an all-zero block),
+// q = e4m3(x / scale) with saturation, written K-major into out[R][Kp];
+// scale into scales[row block][Kp / 128].  One launch quantises both
+// operands of a contraction (blocks of the first, then of the second).  No
+// shared-memory tile: every thread keeps 32 values of the block in
+// registers, coalesced in both layouts:
+//   K-major op(X) (rows contiguous in k): warp w holds rows 8w .. 8w + 7 of
+//     the block, lane l the four k values [4l, 4l + 4) of each (16-byte
+//     loads when the rows are 16-byte aligned and the block is whole in K),
+//     and writes their four E4M3 bytes per row;
+//   MN-major op(X) (op(X)[r][k] = X[k][r]): warp w holds the 32 x 32
+//     sub-block k in [32 (w / 4), +32), r in [32 (w % 4), +32); lane l reads
+//     column r = 32 (w % 4) + l down the 32 k (each load a 128-byte row
+//     segment across the warp), which is 32 consecutive k of output row r:
+//     the transpose happens in the register assignment, and the lane writes
+//     its row's 32 bytes.
+// Only the block maximum crosses warps (one shuffle reduction, 16 words of
+// shared memory).
+struct QuantJob {
+  const float* X;
+  int64_t ld;
+  int k_major, R, K, Kp, kb;  // kb: 128-blocks along K
+  uint8_t* out;
+  float* scales;
+};
+
+__device__ __forceinline__ uint16_t e4m3x2(float a, float b) {
+  return __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+}
+
+__global__ void __launch_bounds__(512, 2) quantize_e4m3_kernel(const QuantJob ja, const QuantJob jb, int blocks_a) {
+  __shared__ float red[16];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool first = int(blockIdx.x) < blocks_a;
+  const QuantJob& j = first ? ja : jb;
+  const int local = first ? int(blockIdx.x) : int(blockIdx.x) - blocks_a;
+  const int rb = local / j.kb, kbi = local % j.kb;
+  const int64_t r0 = int64_t(rb) * 128, k0 = int64_t(kbi) * 128;
+  float x[32];
+  if(j.k_major) {
+    const int64_t kc = k0 + 4 * lane;
+    const bool vec = (j.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(j.X) & 15) == 0 && k0 + 128 <= j.K;
 #pragma unroll
-    for(int e = 0; e < 16; ++e) v[e] = *reinterpret_cast<const float4*>(p + int64_t(e) * 8 * ld);
-    // store j of a float4 writes its element (j + lane / 8) % 4: the warp's
-    // 32 words then fall in 32 different banks (row stride 129)
-    const int rot = (tid >> 3) & 3;
+    for(int i = 0; i < 8; ++i) {
+      const int64_t r = r0 + 8 * warp + i;
+      const float* p = j.X + r * j.ld + kc;
+      if(r < j.R && vec) {
+        const float4 f = *reinterpret_cast<const float4*>(p);
+        x[4 * i] = f.x, x[4 * i + 1] = f.y, x[4 * i + 2] = f.z, x[4 * i + 3] = f.w;
+      } else {
 #pragma unroll
-    for(int e = 0; e < 16; ++e) {
-      const int o = out + 8 * e;
-      amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v[e].x), fabsf(v[e].y)), fmaxf(fabsf(v[e].z), fabsf(v[e].w))));
-#pragma unroll
-      for(int j = 0; j < 4; ++j) {
-        const int q = (j + rot) & 3;
-        const float xq = q == 0 ? v[e].x : (q == 1 ? v[e].y : (q == 2 ? v[e].z : v[e].w));
-        blk[k_major ? o * 129 + in + q : (in + q) * 129 + o] = xq;
+        for(int c = 0; c < 4; ++c) x[4 * i + c] = (r < j.R && kc + c < j.K) ? p[c] : 0.f;
       }
     }
   } else {
-    // element e of the thread: outer index tid / 128 + 2 e, inner tid % 128
-    const int out = tid >> 7, in = tid & 127;
-    const int64_t in_lim = k_major ? K - k0 : R - r0, out_lim = k_major ? R - r0 : K - k0;
-    const float* p = X + (o0 + out) * ld + i0 + in;
+    const int64_t rr = r0 + 32 * (warp & 3) + lane, kk = k0 + 32 * (warp >> 2);
+    const float* p = j.X + kk * j.ld + rr;
 #pragma unroll
-    for(int b = 0; b < 64; b += 16) {
-      float v[16];
-#pragma unroll
-      for(int e = 0; e < 16; ++e)
-        v[e] = (in < in_lim && out + 2 * (b + e) < out_lim) ? p[int64_t(b + e) * 2 * ld] : 0.f;
-#pragma unroll
-      for(int e = 0; e < 16; ++e) {
-        const int o = out + 2 * (b + e);
-        blk[k_major ? o * 129 + in : in * 129 + o] = v[e];
-        amax = fmaxf(amax, fabsf(v[e]));
-      }
-    }
+    for(int i = 0; i < 32; ++i) x[i] = (rr < j.R && kk + i < j.K) ? p[int64_t(i) * j.ld] : 0.f;
   }
+  float amax = 0.f;
+#pragma unroll
+  for(int i = 0; i < 32; ++i) amax = fmaxf(amax, fabsf(x[i]));
 #pragma unroll
   for(int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  if((tid & 31) == 0) red[tid >> 5] = amax;
+  if(lane == 0) red[warp] = amax;
   __syncthreads();
   float m = red[0];
 #pragma unroll
-  for(int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+  for(int w = 1; w < 16; ++w) m = fmaxf(m, red[w]);
   const float scale = m > 0.f ? m / 448.f : 1.f;
   const float inv = 1.f / scale;
-  if(tid == 0) scales[int64_t(blockIdx.y) * (Kp / 128) + blockIdx.x] = scale;
-  // each thread: one row, 64 consecutive k (two threads per row), two values
-  // per conversion (round to nearest, saturating, as one at a time)
-  const int rr = tid >> 1, kc = (tid & 1) * 64;
-  const int64_t r = r0 + rr;
-  if(r >= R) return;
-  __align__(16) __nv_fp8x2_storage_t q[32];
+  if(tid == 0) j.scales[int64_t(rb) * (j.Kp / 128) + kbi] = scale;
+  if(j.k_major) {
 #pragma unroll
-  for(int i = 0; i < 32; ++i)
-    q[i] = __nv_cvt_float2_to_fp8x2(make_float2(blk[rr * 129 + kc + 2 * i] * inv, blk[rr * 129 + kc + 2 * i + 1] * inv),
-        __NV_SATFINITE, __NV_E4M3);
-  uint4* dst = reinterpret_cast<uint4*>(out + r * Kp + k0 + kc);
+    for(int i = 0; i < 8; ++i) {
+      const int64_t r = r0 + 8 * warp + i;
+      if(r >= j.R) continue;
+      const uint32_t q = uint32_t(e4m3x2(x[4 * i] * inv, x[4 * i + 1] * inv)) |
+                         (uint32_t(e4m3x2(x[4 * i + 2] * inv, x[4 * i + 3] * inv)) << 16);
+      *reinterpret_cast<uint32_t*>(j.out + r * j.Kp + k0 + 4 * lane) = q;
+    }
+  } else {
+    const int64_t rr = r0 + 32 * (warp & 3) + lane;
+    if(rr < j.R) {
+      __align__(16) uint16_t q[16];
 #pragma unroll
-  for(int v = 0; v < 4; ++v) dst[v] = reinterpret_cast<const uint4*>(q)[v];
+      for(int i = 0; i < 16; ++i) q[i] = e4m3x2(x[2 * i] * inv, x[2 * i + 1] * inv);
+      uint4* dst = reinterpret_cast<uint4*>(j.out + rr * j.Kp + k0 + 32 * (warp >> 2));
+      dst[0] = reinterpret_cast<const uint4*>(q)[0];
+      dst[1] = reinterpret_cast<const uint4*>(q)[1];
+    }
+  }
 }
 
 // Tensor maps of one product pairing: left operand terms in 128-row boxes,
@@ -1293,22 +1337,14 @@ gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
   uint8_t* qb = same ? qa : reinterpret_cast<uint8_t*>(ws + a_bytes);
   float* sa = reinterpret_cast<float*>(ws + a_bytes + b_bytes);
   float* sb = same ? sa : reinterpret_cast<float*>(ws + a_bytes + b_bytes + sa_bytes);
-  static unsigned attr_q = 0;
-  constexpr int kQSmem = 128 * 129 * 4;
-  if(ctx->device < 32 && !(attr_q & (1u << ctx->device))) {
-    GBPOLY_CUDA_TRY(cudaFuncSetAttribute(quantize_e4m3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kQSmem));
-    attr_q |= 1u << ctx->device;
-  }
   {
     ProfileScope prof(ctx, "quantize_e4m3");
-    quantize_e4m3_kernel<<<dim3(unsigned(kb), unsigned(mb)), 256, kQSmem, ctx->stream>>>(
-        a.A, a.lda, a.op_a == GBPOLY_OP_N ? 1 : 0, int(a.M), int(a.K), int(Kp), qa, sa);
+    const QuantJob ja{a.A, a.lda, a.op_a == GBPOLY_OP_N ? 1 : 0, int(a.M), int(a.K), int(Kp), int(kb), qa, sa};
+    const QuantJob jb{a.B, a.ldb, a.op_b == GBPOLY_OP_T ? 1 : 0, int(a.N), int(a.K), int(Kp), int(kb), qb, sb};
+    const int64_t blocks_a = mb * kb, blocks = blocks_a + (same ? 0 : nb * kb);
+    if(blocks >= (1ll << 31)) return fail(GBPOLY_ERR_UNSUPPORTED, "too many quantisation blocks");
+    quantize_e4m3_kernel<<<unsigned(blocks), 512, 0, ctx->stream>>>(ja, jb, int(blocks_a));
     GBPOLY_CUDA_TRY(cudaGetLastError());
-    if(!same) {
-      quantize_e4m3_kernel<<<dim3(unsigned(kb), unsigned(nb)), 256, kQSmem, ctx->stream>>>(
-          a.B, a.ldb, a.op_b == GBPOLY_OP_T ? 1 : 0, int(a.N), int(a.K), int(Kp), qb, sb);
-      GBPOLY_CUDA_TRY(cudaGetLastError());
-    }
   }
   GemmMaps maps;
   int npair = 1;
@@ -1541,7 +1577,7 @@ struct gbpoly_grouped {
   gbpoly::ProductMaps* maps = nullptr;
   int4* tiles = nullptr;
   gbpoly::SplitJob* jobs = nullptr;
-  int* block_job = nullptr;  // split block -> job
+  int4* split_table = nullptr;  // split block -> (job, row block, k block, 0)
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
   int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3) 128 x 256
@@ -1583,7 +1619,7 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   }
   if(nblocks >= (1ll << 31)) return fail(GBPOLY_ERR_UNSUPPORTED, "too many split blocks in one grouped plan");
   const size_t table_off = align_up(jobs_off + 2 * P * sizeof(SplitJob), 256);
-  const size_t total = table_off + size_t(nblocks) * sizeof(int);
+  const size_t total = table_off + size_t(nblocks) * sizeof(int4);
   GBPOLY_CUDA_TRY(cudaMalloc(&g->dev, total));
   g->dev_bytes = total;
   char* base = static_cast<char*>(g->dev);
@@ -1591,7 +1627,13 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   std::vector<GroupProblem> probs(P);
   std::vector<ProductMaps> maps(P);
   std::vector<SplitJob> jobs;
-  int blocks = 0;
+  std::vector<int4> table;  // split block -> (job, row block, k block, 0), operand by operand
+  table.reserve(size_t(nblocks));
+  auto add_blocks = [&](int64_t rows, int kb) {
+    const int job = int(jobs.size()) - 1;
+    for(int rb = 0; rb < int((rows + 63) / 64); ++rb)
+      for(int k = 0; k < kb; ++k) table.push_back(make_int4(job, rb, k, 0));
+  };
   gbpoly_status st;
   for(int i = 0; i < P; ++i) {
     const auto& d = g->descs[i];
@@ -1602,11 +1644,11 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
       if((st = make_product_maps<F>(ctx, maps[i], pa, d.M, pb, d.N, kp[i])) != GBPOLY_OK) return st;
       const int kb = int(kp[i] / 64);
       jobs.push_back(SplitJob{d.A, d.lda, d.op_a == GBPOLY_OP_N ? 1 : 0, int(d.M), int(d.K), int(kp[i]), pa.base,
-          int64_t(sa / F::esz), blocks, kb});
-      blocks += int((d.M + 63) / 64) * kb;
+          int64_t(sa / F::esz)});
+      add_blocks(d.M, kb);
       jobs.push_back(SplitJob{d.B, d.ldb, d.op_b == GBPOLY_OP_T ? 1 : 0, int(d.N), int(d.K), int(kp[i]), pb.base,
-          int64_t(sb / F::esz), blocks, kb});
-      blocks += int((d.N + 63) / 64) * kb;
+          int64_t(sb / F::esz)});
+      add_blocks(d.N, kb);
     }
     g->flops += 2 * d.M * d.N * d.K;
   }
@@ -1614,18 +1656,12 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   g->maps = reinterpret_cast<ProductMaps*>(base + maps_off);
   g->tiles = reinterpret_cast<int4*>(base + tiles_off);
   g->jobs = reinterpret_cast<SplitJob*>(base + jobs_off);
-  g->block_job = reinterpret_cast<int*>(base + table_off);
+  g->split_table = reinterpret_cast<int4*>(base + table_off);
   g->ntiles = int(tiles.size());
   g->njobs = int(jobs.size());
-  g->split_blocks = blocks;
-  std::vector<int> owner(size_t(blocks), 0);
-  for(size_t jb = 0; jb < jobs.size(); ++jb) {
-    const int first_block = jobs[jb].block_start;
-    const int end_block = jb + 1 < jobs.size() ? jobs[jb + 1].block_start : blocks;
-    std::fill(owner.begin() + first_block, owner.begin() + end_block, int(jb));
-  }
-  if(!owner.empty())
-    GBPOLY_CUDA_TRY(cudaMemcpy(g->block_job, owner.data(), owner.size() * sizeof(int), cudaMemcpyHostToDevice));
+  g->split_blocks = int(table.size());
+  if(!table.empty())
+    GBPOLY_CUDA_TRY(cudaMemcpy(g->split_table, table.data(), table.size() * sizeof(int4), cudaMemcpyHostToDevice));
   GBPOLY_CUDA_TRY(cudaMemcpy(g->probs, probs.data(), P * sizeof(GroupProblem), cudaMemcpyHostToDevice));
   GBPOLY_CUDA_TRY(cudaMemcpy(g->maps, maps.data(), P * sizeof(ProductMaps), cudaMemcpyHostToDevice));
   if(!tiles.empty())
@@ -1642,7 +1678,7 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
     ProfileScope prof(ctx, "grouped_split");
     // persistent: 4 CTAs per SM
     const int ctas = std::min(g->split_blocks, 4 * std::max(1, ctx->sm_count));
-    grouped_split_kernel<F::elem, F::terms><<<ctas, 256, 0, ctx->stream>>>(g->jobs, g->block_job, g->split_blocks);
+    grouped_split_kernel<F::elem, F::terms><<<ctas, 256, 0, ctx->stream>>>(g->jobs, g->split_table, g->split_blocks);
     GBPOLY_CUDA_TRY(cudaGetLastError());
   }
   (void)sizeof(T);
