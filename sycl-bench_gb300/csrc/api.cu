@@ -265,7 +265,6 @@ gbpoly_status gbpoly_destroy(gbpoly_ctx* ctx) {
   for(void* p : {ctx->stage_a, ctx->stage_b, ctx->stage_c})
     if(p) cudaFree(p);
   if(ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
-  if(ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   if(ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
   for(auto& r : ctx->prof) {
     cudaEventDestroy(r.start);

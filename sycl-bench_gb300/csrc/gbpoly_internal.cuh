@@ -80,8 +80,6 @@ struct gbpoly_ctx {
   std::map<std::tuple<int, int, int, int, int>, int> tuned_grouped;
   // host-buffer calls: copy streams and device staging of the operands
   cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
-  // mixed grouped plans: the second branch of the fork (created by the first such plan)
-  cudaStream_t aux_stream = nullptr;
   void *stage_a = nullptr, *stage_b = nullptr, *stage_c = nullptr;
   size_t stage_a_bytes = 0, stage_b_bytes = 0, stage_c_bytes = 0;
 };
@@ -201,7 +199,6 @@ std::tuple<int, int, int, int, int> group_class(gbpoly_precision prec, const gbp
 int default_grouped_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count);
 gbpoly_status grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count,
     int config, gbpoly_grouped** out);
-gbpoly_status plan_mixed(gbpoly_ctx* ctx, gbpoly_grouped* g, int share);
 // Workspace bytes launch_gemm_tensor needs for this shape (0 for FP32).
 size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, bool same_operand);
 

@@ -1230,23 +1230,20 @@ gbpoly_status apply_tail(gbpoly_ctx* ctx, const TailPlan& tp, char* base, S& sch
 // Launch the tensor-core kernel for scheduler S: one persistent CTA (or CTA
 // pair) per SM (pair of SMs), walking `units` work units.
 template <class F, class S>
-gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t units, const char* kernel_name,
-    int max_ctas = 0) {
+gbpoly_status launch_tc_kernel(gbpoly_ctx* ctx, const S& sched, int64_t units, const char* kernel_name) {
   gbpoly_status st = tc_prepare<F, S>(ctx);
   if(st != GBPOLY_OK) return st;
   if(units <= 0) return GBPOLY_OK;
   if constexpr(F::CG == 2) {
     // CTA pairs: a cluster of two per tile, as many clusters as fit at once
-    // (at most max_ctas / 2 when the launch shares the device)
     int P = 0;
     if((st = pair_clusters<F, S>(ctx, P)) != GBPOLY_OK) return st;
-    if(max_ctas > 0) P = std::max(1, std::min(P, max_ctas / 2));
     PairLaunch<F> pl(ctx, int(std::min<int64_t>(units, P)));
     ProfileScope prof(ctx, kernel_name);
     GBPOLY_CUDA_TRY(cudaLaunchKernelEx(&pl.cfg, split_gemm_kernel<F, S>, sched, ctx->err_dev));
     return GBPOLY_OK;
   }
-  const int grid = int(std::min<int64_t>(units, max_ctas > 0 ? std::min(max_ctas, ctx->sm_count) : ctx->sm_count));
+  const int grid = int(std::min<int64_t>(units, ctx->sm_count));
   ProfileScope prof(ctx, kernel_name);
   split_gemm_kernel<F, S><<<grid, F::THREADS, F::SMEM, ctx->stream>>>(sched, ctx->err_dev);
   GBPOLY_CUDA_TRY(cudaGetLastError());
@@ -1597,14 +1594,7 @@ struct gbpoly_grouped {
   int4* split_table = nullptr;  // split block -> (job, row block, k block, 0)
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
-  int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3) 128 x 256, then mixed
-  int max_ctas = 0;  // CTAs of the persistent launch (0: every SM)
-  // mixed configurations: the problems that 256 x 256 tiles pad little run
-  // on CTA pairs (sub[0]), the rest on 1-CTA 128 x 128 tiles (sub[1]), as two
-  // concurrent branches (fork on the context's stream, join back) on disjoint
-  // shares of the SMs
-  gbpoly_grouped* sub[2] = {nullptr, nullptr};
-  cudaEvent_t fork = nullptr, join = nullptr;
+  int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3) 128 x 256
 };
 
 namespace gbpoly {
@@ -1707,7 +1697,7 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
   }
   (void)sizeof(T);
   GroupedSched<F::BM, F::BN> sched{g->probs, g->maps, g->tiles, g->ntiles};
-  return launch_tc_kernel<F>(ctx, sched, g->ntiles, name, g->max_ctas);
+  return launch_tc_kernel<F>(ctx, sched, g->ntiles, name);
 }
 
 // Tile configurations of grouped plans: 0 = 1-CTA 128 x 128 tiles (least
@@ -1742,8 +1732,7 @@ bool grouped_pairs(gbpoly_ctx* ctx, const std::vector<gbpoly_gemm_desc>& descs) 
 
 }  // namespace
 
-// Single-launch configurations of a form; the mixed ones follow them.
-int grouped_base_configs(gbpoly_precision prec) {
+int grouped_config_count(gbpoly_precision prec) {
   switch(prec) {
   case GBPOLY_PREC_BF16X3: return 3;
   case GBPOLY_PREC_TF32X3:
@@ -1751,24 +1740,6 @@ int grouped_base_configs(gbpoly_precision prec) {
   case GBPOLY_PREC_TF32: return 2;
   default: return 0;
   }
-}
-
-// Mixed configuration m: the share of the SMs given to the CTA-pair branch.
-constexpr int kMixedShares = 3;
-constexpr double kMixedShare[kMixedShares] = {0.5, 2.0 / 3.0, 5.0 / 6.0};
-
-int grouped_config_count(gbpoly_precision prec) {
-  const int base = grouped_base_configs(prec);
-  return base ? base + kMixedShares : 0;
-}
-
-// A problem whose 256 x 256 tiles pad its output at most 10 % more than
-// 128 x 128 tiles do runs on CTA pairs in the mixed configurations.
-bool pair_problem(const gbpoly_gemm_desc& d) {
-  if(d.M <= 0 || d.N <= 0) return false;
-  const double w128 = double((d.M + 127) / 128 * 128) * double((d.N + 127) / 128 * 128);
-  const double w256 = double((d.M + 255) / 256 * 256) * double((d.N + 255) / 256 * 256);
-  return w256 <= 1.1 * w128;
 }
 
 int default_grouped_config(gbpoly_ctx* ctx, gbpoly_precision prec, const gbpoly_gemm_desc* descs, int count) {
@@ -1840,10 +1811,6 @@ gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec
       st = fail(GBPOLY_ERR_INVALID, "no such grouped tile configuration");
       break;
     }
-    if(g->config >= grouped_base_configs(prec)) {
-      st = plan_mixed(ctx, g, g->config - grouped_base_configs(prec));
-      break;
-    }
     switch(prec * 4 + g->config) {
     case GBPOLY_PREC_BF16X3 * 4: st = plan_grouped<GroupBF16x3>(ctx, g); break;
     case GBPOLY_PREC_BF16X3 * 4 + 1: st = plan_grouped<GroupBF16x3_p>(ctx, g); break;
@@ -1859,41 +1826,11 @@ gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec
   default: st = fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   }
   if(st != GBPOLY_OK) {
-    gbpoly_grouped_destroy(nullptr, g);
+    if(g->dev) cudaFree(g->dev);
+    delete g;
     return st;
   }
   *out = g;
-  return GBPOLY_OK;
-}
-
-// Mixed configuration: two sub-plans (CTA pairs for the problems that
-// pair_problem admits, 1-CTA 128 x 128 tiles for the rest), each limited to
-// its share of the SMs.  A group that is all one kind runs as one plan of
-// that kind on every SM.
-gbpoly_status gbpoly::plan_mixed(gbpoly_ctx* ctx, gbpoly_grouped* g, int share) {
-  std::vector<gbpoly_gemm_desc> big, small;
-  for(const auto& d : g->descs) (pair_problem(d) ? big : small).push_back(d);
-  if(big.empty() || small.empty()) {
-    gbpoly_grouped* one = nullptr;
-    gbpoly_status st =
-        grouped_plan_config(ctx, g->prec, g->descs.data(), int(g->descs.size()), big.empty() ? 0 : 1, &one);
-    if(st != GBPOLY_OK) return st;
-    g->sub[0] = one;
-    g->flops = one->flops;
-    g->ntiles = one->ntiles;
-    return GBPOLY_OK;
-  }
-  gbpoly_status st = grouped_plan_config(ctx, g->prec, big.data(), int(big.size()), 1, &g->sub[0]);
-  if(st == GBPOLY_OK) st = grouped_plan_config(ctx, g->prec, small.data(), int(small.size()), 0, &g->sub[1]);
-  if(st != GBPOLY_OK) return st;
-  const int pair_ctas = std::max(2, 2 * int(kMixedShare[share] * ctx->sm_count / 2));
-  g->sub[0]->max_ctas = pair_ctas;
-  g->sub[1]->max_ctas = std::max(1, ctx->sm_count - pair_ctas);
-  g->flops = g->sub[0]->flops + g->sub[1]->flops;
-  g->ntiles = g->sub[0]->ntiles + g->sub[1]->ntiles;
-  if(!ctx->aux_stream) GBPOLY_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
-  GBPOLY_CUDA_TRY(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
-  GBPOLY_CUDA_TRY(cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming));
   return GBPOLY_OK;
 }
 
@@ -1904,21 +1841,6 @@ gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   if(!ctx || !g) return fail(GBPOLY_ERR_INVALID, "bad argument");
   if(g->descs.empty()) return GBPOLY_OK;
   GBPOLY_CUDA_TRY(cudaSetDevice(ctx->device));
-  if(g->sub[0] && !g->sub[1]) return gbpoly_grouped_run(ctx, g->sub[0]);
-  if(g->sub[0]) {
-    // fork: the pairs branch on the context's stream, the 128 x 128 branch on
-    // the auxiliary stream, each on its share of the SMs; join back
-    GBPOLY_CUDA_TRY(cudaEventRecord(g->fork, ctx->stream));
-    GBPOLY_CUDA_TRY(cudaStreamWaitEvent(ctx->aux_stream, g->fork, 0));
-    gbpoly_status st = gbpoly_grouped_run(ctx, g->sub[0]);
-    cudaStream_t main = ctx->stream;
-    ctx->stream = ctx->aux_stream;
-    gbpoly_status st2 = gbpoly_grouped_run(ctx, g->sub[1]);
-    ctx->stream = main;
-    GBPOLY_CUDA_TRY(cudaEventRecord(g->join, ctx->aux_stream));
-    GBPOLY_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, g->join, 0));
-    return st != GBPOLY_OK ? st : st2;
-  }
   switch(g->prec) {
   case GBPOLY_PREC_FP32:
     for(const auto& d : g->descs) {
@@ -1964,11 +1886,8 @@ gbpoly_status gbpoly_grouped_destroy(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   if(!g) return GBPOLY_OK;
   if(ctx) {
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);  // a mixed plan's branches joined back into it
+    cudaStreamSynchronize(ctx->stream);
   }
-  for(auto* sub : g->sub) gbpoly_grouped_destroy(nullptr, sub);
-  if(g->fork) cudaEventDestroy(g->fork);
-  if(g->join) cudaEventDestroy(g->join);
   if(g->dev) cudaFree(g->dev);
   delete g;
   return GBPOLY_OK;

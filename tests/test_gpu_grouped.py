@@ -215,40 +215,3 @@ def test_grouped_autotune_records_and_persists(ctx, tmp_path):
     for b in bufs:
         for x in b:
             ctx.free(x)
-
-
-@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.TF32X3])
-def test_mixed_configuration_in_a_graph(ctx, prec):
-    """A mixed configuration (large problems on CTA pairs, the rest on
-    128 x 128 tiles, as two concurrent branches forked from the context's
-    stream) captured into a CUDA graph replays its eager result bit for bit,
-    and matches FP64 per problem."""
-    rng = np.random.default_rng(35)
-    probs = make_problems(rng, 16, 64, 300) + make_problems(rng, 4, 900, 1400)[:4]
-    descs, bufs = group_descs(ctx, probs)
-    mixed = ctx.grouped_config_count(prec) - 1
-    ctx.grouped_config_set(prec, descs, mixed)
-    plan = ctx.grouped_plan(prec, descs)
-    assert ctx.grouped_config_of(plan) == mixed
-    ctx.grouped_run(plan)
-    ctx.synchronize()
-    eager = [ctx.download(b[2], (p[2], p[3])) for p, b in zip(probs, bufs)]
-    for (op_a, op_b, M, N, K, A, B, C), e in zip(probs, eager):
-        ref = oracle.gemm_f64(A, B, C, 1.0, 0.5, op_a=int(op_a), op_b=int(op_b)) if K else 0.5 * C.astype(np.float64)
-        assert oracle.error_norms(e, ref)[1] < BOUND[prec], (M, N, K)
-    ctx.graph_begin()
-    try:
-        ctx.grouped_run(plan)
-    finally:
-        g = ctx.graph_end()
-    for p, b in zip(probs, bufs):
-        ctx.h2d(b[2], p[7])
-    ctx.graph_launch(g)
-    ctx.synchronize()
-    for e, p, b in zip(eager, probs, bufs):
-        np.testing.assert_array_equal(ctx.download(b[2], (p[2], p[3])), e)
-    ctx.graph_destroy(g)
-    ctx.grouped_destroy(plan)
-    for b in bufs:
-        for x in b:
-            ctx.free(x)
