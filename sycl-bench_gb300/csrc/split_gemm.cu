@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
 }
 
 // ---------------------------------------------------------- FP8 quantize --
-// 128 x 128 blocks of op(X) (rows x K, zero beyond R and K), one per CTA of
-// 512 threads: scale = max|x| / 448 (1 for an all-zero block),
+// 128 x 128 blocks of op(X) (rows x K, zero beyond R and K), walked by
+// persistent CTAs of 512 threads (two per SM), one block at a time: scale = max|x| / 448 (1 for an all-zero block),
 // q = e4m3(x / scale) with saturation, written K-major into out[R][Kp];
 // scale into scales[row block][Kp / 128].  One launch quantises both
 // operands of a contraction (blocks of the first, then of the second).  No
@@ -474,68 +474,72 @@ __device__ __forceinline__ uint16_t e4m3x2(float a, float b) {
   return __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
 }
 
-__global__ void __launch_bounds__(512, 2) quantize_e4m3_kernel(const QuantJob ja, const QuantJob jb, int blocks_a) {
+__global__ void __launch_bounds__(512, 2) quantize_e4m3_kernel(const QuantJob ja, const QuantJob jb, int blocks_a,
+    int nblocks) {
   __shared__ float red[16];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool first = int(blockIdx.x) < blocks_a;
-  const QuantJob& j = first ? ja : jb;
-  const int local = first ? int(blockIdx.x) : int(blockIdx.x) - blocks_a;
-  const int rb = local / j.kb, kbi = local % j.kb;
-  const int64_t r0 = int64_t(rb) * 128, k0 = int64_t(kbi) * 128;
-  float x[32];
-  if(j.k_major) {
-    const int64_t kc = k0 + 4 * lane;
-    const bool vec = (j.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(j.X) & 15) == 0 && k0 + 128 <= j.K;
+  for(int blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    const bool first = blk < blocks_a;
+    const QuantJob& j = first ? ja : jb;
+    const int local = first ? blk : blk - blocks_a;
+    const int rb = local / j.kb, kbi = local % j.kb;
+    const int64_t r0 = int64_t(rb) * 128, k0 = int64_t(kbi) * 128;
+    float x[32];
+    if(j.k_major) {
+      const int64_t kc = k0 + 4 * lane;
+      const bool vec = (j.ld & 3) == 0 && (reinterpret_cast<uintptr_t>(j.X) & 15) == 0 && k0 + 128 <= j.K;
 #pragma unroll
-    for(int i = 0; i < 8; ++i) {
-      const int64_t r = r0 + 8 * warp + i;
-      const float* p = j.X + r * j.ld + kc;
-      if(r < j.R && vec) {
-        const float4 f = *reinterpret_cast<const float4*>(p);
-        x[4 * i] = f.x, x[4 * i + 1] = f.y, x[4 * i + 2] = f.z, x[4 * i + 3] = f.w;
-      } else {
+      for(int i = 0; i < 8; ++i) {
+        const int64_t r = r0 + 8 * warp + i;
+        const float* p = j.X + r * j.ld + kc;
+        if(r < j.R && vec) {
+          const float4 f = *reinterpret_cast<const float4*>(p);
+          x[4 * i] = f.x, x[4 * i + 1] = f.y, x[4 * i + 2] = f.z, x[4 * i + 3] = f.w;
+        } else {
 #pragma unroll
-        for(int c = 0; c < 4; ++c) x[4 * i + c] = (r < j.R && kc + c < j.K) ? p[c] : 0.f;
+          for(int c = 0; c < 4; ++c) x[4 * i + c] = (r < j.R && kc + c < j.K) ? p[c] : 0.f;
+        }
+      }
+    } else {
+      const int64_t rr = r0 + 32 * (warp & 3) + lane, kk = k0 + 32 * (warp >> 2);
+      const float* p = j.X + kk * j.ld + rr;
+#pragma unroll
+      for(int i = 0; i < 32; ++i) x[i] = (rr < j.R && kk + i < j.K) ? p[int64_t(i) * j.ld] : 0.f;
+    }
+    float amax = 0.f;
+#pragma unroll
+    for(int i = 0; i < 32; ++i) amax = fmaxf(amax, fabsf(x[i]));
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if(lane == 0) red[warp] = amax;
+    __syncthreads();
+    float m = red[0];
+#pragma unroll
+    for(int w = 1; w < 16; ++w) m = fmaxf(m, red[w]);
+    const float scale = m > 0.f ? m / 448.f : 1.f;
+    const float inv = 1.f / scale;
+    if(tid == 0) j.scales[int64_t(rb) * (j.Kp / 128) + kbi] = scale;
+    if(j.k_major) {
+#pragma unroll
+      for(int i = 0; i < 8; ++i) {
+        const int64_t r = r0 + 8 * warp + i;
+        if(r >= j.R) continue;
+        const uint32_t q = uint32_t(e4m3x2(x[4 * i] * inv, x[4 * i + 1] * inv)) |
+                           (uint32_t(e4m3x2(x[4 * i + 2] * inv, x[4 * i + 3] * inv)) << 16);
+        *reinterpret_cast<uint32_t*>(j.out + r * j.Kp + k0 + 4 * lane) = q;
+      }
+    } else {
+      const int64_t rr = r0 + 32 * (warp & 3) + lane;
+      if(rr < j.R) {
+        __align__(16) uint16_t q[16];
+#pragma unroll
+        for(int i = 0; i < 16; ++i) q[i] = e4m3x2(x[2 * i] * inv, x[2 * i + 1] * inv);
+        uint4* dst = reinterpret_cast<uint4*>(j.out + rr * j.Kp + k0 + 32 * (warp >> 2));
+        dst[0] = reinterpret_cast<const uint4*>(q)[0];
+        dst[1] = reinterpret_cast<const uint4*>(q)[1];
       }
     }
-  } else {
-    const int64_t rr = r0 + 32 * (warp & 3) + lane, kk = k0 + 32 * (warp >> 2);
-    const float* p = j.X + kk * j.ld + rr;
-#pragma unroll
-    for(int i = 0; i < 32; ++i) x[i] = (rr < j.R && kk + i < j.K) ? p[int64_t(i) * j.ld] : 0.f;
-  }
-  float amax = 0.f;
-#pragma unroll
-  for(int i = 0; i < 32; ++i) amax = fmaxf(amax, fabsf(x[i]));
-#pragma unroll
-  for(int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  if(lane == 0) red[warp] = amax;
-  __syncthreads();
-  float m = red[0];
-#pragma unroll
-  for(int w = 1; w < 16; ++w) m = fmaxf(m, red[w]);
-  const float scale = m > 0.f ? m / 448.f : 1.f;
-  const float inv = 1.f / scale;
-  if(tid == 0) j.scales[int64_t(rb) * (j.Kp / 128) + kbi] = scale;
-  if(j.k_major) {
-#pragma unroll
-    for(int i = 0; i < 8; ++i) {
-      const int64_t r = r0 + 8 * warp + i;
-      if(r >= j.R) continue;
-      const uint32_t q = uint32_t(e4m3x2(x[4 * i] * inv, x[4 * i + 1] * inv)) |
-                         (uint32_t(e4m3x2(x[4 * i + 2] * inv, x[4 * i + 3] * inv)) << 16);
-      *reinterpret_cast<uint32_t*>(j.out + r * j.Kp + k0 + 4 * lane) = q;
-    }
-  } else {
-    const int64_t rr = r0 + 32 * (warp & 3) + lane;
-    if(rr < j.R) {
-      __align__(16) uint16_t q[16];
-#pragma unroll
-      for(int i = 0; i < 16; ++i) q[i] = e4m3x2(x[2 * i] * inv, x[2 * i + 1] * inv);
-      uint4* dst = reinterpret_cast<uint4*>(j.out + rr * j.Kp + k0 + 32 * (warp >> 2));
-      dst[0] = reinterpret_cast<const uint4*>(q)[0];
-      dst[1] = reinterpret_cast<const uint4*>(q)[1];
-    }
+    __syncthreads();  // red[] is read by every thread before the next block writes it
   }
 }
 
@@ -1357,7 +1361,9 @@ gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
     const QuantJob jb{a.B, a.ldb, a.op_b == GBPOLY_OP_T ? 1 : 0, int(a.N), int(a.K), int(Kp), int(kb), qb, sb};
     const int64_t blocks_a = mb * kb, blocks = blocks_a + (same ? 0 : nb * kb);
     if(blocks >= (1ll << 31)) return fail(GBPOLY_ERR_UNSUPPORTED, "too many quantisation blocks");
-    quantize_e4m3_kernel<<<unsigned(blocks), 512, 0, ctx->stream>>>(ja, jb, int(blocks_a));
+    // persistent: two CTAs per SM walk the blocks (no launch and drain per block)
+    const unsigned ctas = unsigned(std::min<int64_t>(blocks, 2 * int64_t(std::max(1, ctx->sm_count))));
+    quantize_e4m3_kernel<<<ctas, 512, 0, ctx->stream>>>(ja, jb, int(blocks_a), int(blocks));
     GBPOLY_CUDA_TRY(cudaGetLastError());
   }
   GemmMaps maps;
