@@ -53,6 +53,35 @@ gbpoly_status ensure_scratch(gbpoly_ctx* ctx, Workspace& w, size_t bytes, const 
 gbpoly_status ensure_workspace(gbpoly_ctx* ctx, size_t bytes) { return ensure_scratch(ctx, ctx->ws, bytes, "workspace"); }
 
 namespace {
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+std::atomic<PfnCtxGetCurrent> g_ctx_get_current{nullptr};
+std::atomic<PfnCtxGetId> g_ctx_get_id{nullptr};
+std::atomic<bool> g_ctx_fns_resolved{false};
+}  // namespace
+
+unsigned long long current_context_id() {
+  if(!g_ctx_fns_resolved.load(std::memory_order_acquire)) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current.store(reinterpret_cast<PfnCtxGetCurrent>(fn));
+    fn = nullptr;
+    if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_id.store(reinterpret_cast<PfnCtxGetId>(fn));
+    g_ctx_fns_resolved.store(true, std::memory_order_release);
+  }
+  const PfnCtxGetCurrent get_current = g_ctx_get_current.load();
+  const PfnCtxGetId get_id = g_ctx_get_id.load();
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if(!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+namespace {
 cudaEvent_t pooled_event(gbpoly_ctx* ctx) {
   if(!ctx->event_pool.empty()) {
     cudaEvent_t e = ctx->event_pool.back();

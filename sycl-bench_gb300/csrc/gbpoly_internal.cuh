@@ -12,6 +12,7 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <tuple>
@@ -107,6 +108,29 @@ public:
 private:
   gbpoly_ctx* ctx_;
   size_t index_ = size_t(-1);
+};
+
+// Process-unique id of the calling thread's current CUDA context
+// (cuCtxGetId), 0 when the driver does not report one.
+unsigned long long current_context_id();
+
+// Set-up that belongs to a device's context (a kernel's shared-memory
+// opt-in, an occupancy figure, a symbol's device address) is done once per
+// device and remembered with the id of the context it was done in; after
+// cudaDeviceReset the device has a new context, valid() is false again and
+// the set-up is repeated.  Devices beyond 31 are never remembered (set-up on
+// every call).
+class ContextMark {
+public:
+  bool valid(int device) const {
+    return device >= 0 && device < 32 && id_[device].load(std::memory_order_acquire) == current_context_id() + 1;
+  }
+  void set(int device) {
+    if(device >= 0 && device < 32) id_[device].store(current_context_id() + 1, std::memory_order_release);
+  }
+
+private:
+  std::atomic<unsigned long long> id_[32] = {};  // context id + 1 of the set-up; 0: none
 };
 
 // Grow the context workspace to at least `bytes` (synchronises when it grows;

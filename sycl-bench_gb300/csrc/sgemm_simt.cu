@@ -346,10 +346,10 @@ gbpoly_status launch_tma(gbpoly_ctx* ctx, const GemmF32Args& a, const CUtensorMa
   constexpr int kStageBytes = (DUAL ? 4 : 2) * kTileBytes;
   constexpr int kSmem = STAGES * kStageBytes + 1024 + 2 * STAGES * 8;
   auto kern = sgemm_tma_kernel<A_KMAJ, B_KMAJ, DUAL, STAGES>;
-  static unsigned attr_set = 0;  // one bit per device: the attribute is set once per device
-  if(ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
+  static ContextMark attr_set;  // the attribute is set once per device context
+  if(!attr_set.valid(ctx->device)) {
     GBPOLY_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem));
-    attr_set |= 1u << ctx->device;
+    attr_set.set(ctx->device);
   }
   int64_t tiles = ((a.M + kBM - 1) / kBM) * ((a.N + kBN - 1) / kBN);
   if(lower) {

@@ -1122,12 +1122,12 @@ gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, i
   return GBPOLY_OK;
 }
 
-// One-time per device: shared-memory opt-in and the register check of the
-// warp split.
+// Once per device context: shared-memory opt-in and the register check of
+// the warp split.
 template <class F, class S>
 gbpoly_status tc_prepare(gbpoly_ctx* ctx) {
-  static unsigned attr_set = 0;
-  if(ctx->device < 32 && (attr_set & (1u << ctx->device))) return GBPOLY_OK;
+  static ContextMark prepared;
+  if(prepared.valid(ctx->device)) return GBPOLY_OK;
   GBPOLY_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<F, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, F::SMEM));
   // setmaxnreg redistributes the registers the CTA was launched with: the
   // split must fit in threads x registers-per-thread at launch, or the
@@ -1137,7 +1137,7 @@ gbpoly_status tc_prepare(gbpoly_ctx* ctx) {
   const long need = 128l * F::REGS_CTRL + 256l * F::REGS_EPI;
   if(long(fa.numRegs) * F::THREADS < need)
     return fail(GBPOLY_ERR_UNSUPPORTED, "tensor-core kernel built with too few registers for its warp split");
-  if(ctx->device < 32) attr_set |= 1u << ctx->device;
+  prepared.set(ctx->device);
   return GBPOLY_OK;
 }
 
@@ -1160,13 +1160,15 @@ struct PairLaunch {
   }
 };
 
-// CTA pairs of configuration F resident at once on the device (cached).
+// CTA pairs of configuration F resident at once on the device (cached per
+// device context).
 template <class F, class S>
 gbpoly_status pair_clusters(gbpoly_ctx* ctx, int& clusters) {
   static int max_clusters[32] = {};
+  static ContextMark known;
   gbpoly_status st = tc_prepare<F, S>(ctx);
   if(st != GBPOLY_OK) return st;
-  if(ctx->device < 32 && max_clusters[ctx->device] > 0) {
+  if(known.valid(ctx->device)) {
     clusters = max_clusters[ctx->device];
     return GBPOLY_OK;
   }
@@ -1174,7 +1176,10 @@ gbpoly_status pair_clusters(gbpoly_ctx* ctx, int& clusters) {
   int n = 0;
   GBPOLY_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, split_gemm_kernel<F, S>, &pl.cfg));
   if(n <= 0) return fail(GBPOLY_ERR_UNSUPPORTED, "no CTA pair of this tensor-core configuration fits on the device");
-  if(ctx->device < 32) max_clusters[ctx->device] = n;
+  if(ctx->device >= 0 && ctx->device < 32) {
+    max_clusters[ctx->device] = n;
+    known.set(ctx->device);
+  }
   clusters = n;
   return GBPOLY_OK;
 }
@@ -1941,33 +1946,6 @@ struct NoAllocAddr {
   void* ptr = nullptr;
 };
 NoAllocAddr g_noalloc_addr[64];
-
-using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
-using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
-
-// Process-unique id of the calling thread's current context (cuCtxGetId), 0
-// when the driver does not report one.
-unsigned long long current_context_id() {
-  static PfnCtxGetCurrent get_current = nullptr;
-  static PfnCtxGetId get_id = nullptr;
-  static bool resolved = false;
-  if(!resolved) {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_current = reinterpret_cast<PfnCtxGetCurrent>(fn);
-    fn = nullptr;
-    if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_id = reinterpret_cast<PfnCtxGetId>(fn);
-    resolved = true;
-  }
-  CUcontext c = nullptr;
-  unsigned long long id = 0;
-  if(!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
-  return id;
-}
 
 gbpoly_status noalloc_scratch(int device, char** out) {
   if(device < 0 || device >= 64) return fail(GBPOLY_ERR_UNSUPPORTED, "device index beyond 63");
