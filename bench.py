@@ -420,8 +420,9 @@ def run_gpu(args, dist: Dist) -> dict | None:
                 "peak_source": f"computed: {props['sm_count']} SMs x 128 FFMA lanes x 2 x {clk_mhz:.0f} MHz"}
     else:
         # BF16-MMA equivalents per algorithmic multiply-add (a TF32 MMA runs at half the BF16 rate):
-        # bf16x3 3, tf32x3 and bf16x6 6, tf32 2.  The form's ceiling is the BF16 peak divided by that.
-        mma_per_mac = {Precision.BF16X3: 3, Precision.TF32X3: 6, Precision.BF16X6: 6, Precision.TF32: 2,
+        # bf16x3 and fp16x3 3, tf32x3 and bf16x6 6, tf32 2.  The form's ceiling is the BF16 peak divided by that.
+        mma_per_mac = {Precision.BF16X3: 3, Precision.FP16X3: 3, Precision.TF32X3: 6, Precision.BF16X6: 6,
+                       Precision.TF32: 2,
                        Precision.FP8: 0.5}[headline]
         bf16 = peaks["bf16_tflops"]
         peak = bf16 / mma_per_mac
@@ -491,7 +492,7 @@ def run_family(ctx, args) -> dict:
             "i(j+3)": (i * (j + np.float32(3))) / nf}
     dev = {k: ctx.upload(v) for k, v in mats.items()}
     del mats
-    forms = [Precision.FP32, Precision.BF16X3, Precision.BF16X6]
+    forms = [Precision.FP32, Precision.BF16X3, Precision.BF16X6, Precision.FP16X3]
     work = [ctx.alloc(nb) for _ in range(3)]
     ref64 = [ctx.alloc(2 * nb) for _ in range(4)]
     out = {"size": n}
@@ -562,8 +563,8 @@ def run_family(ctx, args) -> dict:
     E, F, G = work
     res = {}
     for prec in forms:
-        # the split forms: E and F (independent) as one grouped launch, then G
-        plan = None if prec == Precision.FP32 else ctx.grouped_plan(prec, ctx.descs([
+        # the split forms with a grouped kernel: E and F (independent) as one grouped launch, then G
+        plan = None if prec in (Precision.FP32, Precision.FP16X3) else ctx.grouped_plan(prec, ctx.descs([
             {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": A, "lda": n, "B": B, "ldb": n, "C": E, "ldc": n},
             {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": Cm, "lda": n, "B": D, "ldb": n, "C": F,
              "ldc": n}]))
@@ -580,7 +581,8 @@ def run_family(ctx, args) -> dict:
         r = {"stage1_E": err(E, c64), "stage2_F": err(F, e64), "end_to_end_G": err(G, g64)}
         g = graph_of(stages) if prec != Precision.FP32 else None
         r.update(time_steps((lambda: ctx.graph_launch(g)) if g else stages, 6.0 * n ** 3))
-        r["mode"] = "grouped E,F + G in one CUDA graph" if g else "three launches"
+        r["mode"] = ("grouped E,F + G in one CUDA graph" if plan is not None else "three launches in one CUDA graph") \
+            if g else "three launches"
         if g:
             ctx.graph_destroy(g)
         if plan is not None:
@@ -1107,7 +1109,7 @@ def main() -> None:
     ap.add_argument("--no-small-k", action="store_true", help="skip the small-K (HBM-bound) GEMM section")
     ap.add_argument("--no-neighbours", action="store_true",
                     help="skip covariance/correlation/matmulchain/matrix-vector section")
-    ap.add_argument("--forms", default="fp32,bf16x3,tf32x3,bf16x6,tf32,fp8", help="forms to time (comma list)")
+    ap.add_argument("--forms", default="fp32,bf16x3,tf32x3,bf16x6,fp16x3,tf32,fp8", help="forms to time (comma list)")
     ap.add_argument("--tile-config", type=int, default=None, help="force this tile configuration (no autotuning)")
     ap.add_argument("--family-size", type=int, default=4096)
     args = ap.parse_args()

@@ -48,7 +48,9 @@ typedef enum {
   GBPOLY_PREC_TF32 = 2,   /* tcgen05 kind::tf32, FP32 accumulation */
   GBPOLY_PREC_FP8 = 3,    /* e4m3 with one scale per 128x128 operand tile */
   GBPOLY_PREC_TF32X3 = 4, /* split-TF32: hi*hi + hi*lo + lo*hi on kind::tf32 (hi+lo keep ~24 bits: FP32-level error) */
-  GBPOLY_PREC_BF16X6 = 5  /* three-way split-BF16: the 6 products of order <= 2^-16 (FP32-level error) */
+  GBPOLY_PREC_BF16X6 = 5, /* three-way split-BF16: the 6 products of order <= 2^-16 (FP32-level error) */
+  GBPOLY_PREC_FP16X3 = 6  /* split-FP16 with one power-of-two scale per 64x64 operand block: hi*hi + hi*lo + lo*hi
+                             (hi+lo keep 22 bits: FP32-level error at bf16x3's speed) */
 } gbpoly_precision;
 
 /* Operand transposition: OP_N uses the matrix as stored, OP_T its transpose. */

@@ -582,6 +582,7 @@ gbpoly_status gbpoly_gemm_f32(gbpoly_ctx* ctx, gbpoly_precision prec, gbpoly_op 
   case GBPOLY_PREC_TF32:
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6:
+  case GBPOLY_PREC_FP16X3:
   case GBPOLY_PREC_FP8: return launch_gemm_tensor(ctx, prec, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
   }
@@ -610,6 +611,7 @@ gbpoly_status gbpoly_syr2k_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N
   case GBPOLY_PREC_TF32:
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6:
+  case GBPOLY_PREC_FP16X3:
   case GBPOLY_PREC_FP8: return launch_gemm_tensor(ctx, prec, a);
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision not available in this build");
   }

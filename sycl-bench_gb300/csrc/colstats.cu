@@ -234,7 +234,7 @@ gbpoly_status gbpoly_covariance_f32(gbpoly_ctx* ctx, gbpoly_precision prec, int6
   a.M = cols, a.N = cols, a.K = rows, a.alpha = 1.f, a.beta = 0.f, a.op_a = GBPOLY_OP_T, a.op_b = GBPOLY_OP_N;
   a.C = C, a.ldc = ldc;
   const bool split_form = prec == GBPOLY_PREC_TF32 || prec == GBPOLY_PREC_BF16X3 || prec == GBPOLY_PREC_TF32X3 ||
-                          prec == GBPOLY_PREC_BF16X6;
+                          prec == GBPOLY_PREC_BF16X6 || prec == GBPOLY_PREC_FP16X3;
   if(split_form && rows > 0) {
     // centred in the split pass: X itself is both operands
     a.A = X, a.lda = ldx, a.B = X, a.ldb = ldx;

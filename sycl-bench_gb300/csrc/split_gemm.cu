@@ -45,6 +45,7 @@
 //     into the same accumulator.
 // All mbarrier waits are bounded (gbpoly_internal.cuh).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_fp8.h>
 #include <stdio.h>
 
@@ -58,7 +59,7 @@
 namespace gbpoly {
 namespace {
 
-enum class Elem { BF16, TF32, E4M3 };
+enum class Elem { BF16, TF32, E4M3, F16 };
 
 // Instruction descriptor of an M x N MMA of element type E (FP32 accumulation).
 template <Elem E, int M, int N>
@@ -66,7 +67,8 @@ constexpr uint32_t idesc_of() {
   if constexpr(E == Elem::E4M3)
     return umma::InstrDescE4M3<M, N>::value;
   else
-    return umma::InstrDesc<M, N, E == Elem::BF16 ? umma::AbType::BF16 : umma::AbType::TF32>::value;
+    return umma::InstrDesc<M, N,
+        E == Elem::BF16 ? umma::AbType::BF16 : (E == Elem::F16 ? umma::AbType::F16 : umma::AbType::TF32)>::value;
 }
 
 // CG_ = 2: a CTA pair (cluster of two) computes a (256 x BN) tile with
@@ -85,12 +87,15 @@ struct Form {
   static constexpr int BM_CTA = 128, BM = BM_CTA * CG;   // rows per CTA; rows of a (pair) tile
   static constexpr int BN_CTA = BN / CG;                 // B rows staged per CTA
   static constexpr int ROW = ROW_;                       // bytes of K per smem row (= swizzle width)
-  static constexpr int esz = E == Elem::BF16 ? 2 : (E == Elem::TF32 ? 4 : 1);
+  static constexpr int esz = (E == Elem::BF16 || E == Elem::F16) ? 2 : (E == Elem::TF32 ? 4 : 1);
   static constexpr int BK = ROW / esz;                   // K elements per stage
   static constexpr int KMMA = 32 / esz;                  // K of one tcgen05.mma (32 bytes)
-  // E4M3 operands carry one scale per 128 x 128 block: a stage (128 bytes of
-  // K) is exactly one block along K, so each TMEM chunk has one scale.
-  static constexpr bool scaled = E == Elem::E4M3;
+  // E4M3 operands carry one scale per 128 x 128 block, F16 terms one
+  // power-of-two scale per 64 x 64 block: a stage (128 bytes of K) is exactly
+  // one block along K, so each TMEM chunk has one scale per SCALE_ROWS rows
+  // of either operand.
+  static constexpr bool scaled = E == Elem::E4M3 || E == Elem::F16;
+  static constexpr int SCALE_ROWS = E == Elem::F16 ? 64 : 128;
   static constexpr int A_TILE = BM_CTA * ROW, B_TILE = BN_CTA * ROW;
   static constexpr int STAGE = TERMS * (A_TILE + B_TILE);  // bytes per stage in each CTA
   static constexpr int STAGE_TX = CG * STAGE;              // bytes a stage's barrier waits for (both CTAs)
@@ -118,7 +123,7 @@ struct Form {
   static constexpr uint32_t REGS_CTRL = 56, REGS_EPI = 208;
   static constexpr uint32_t IDESC = idesc_of<E, BM, BN>();
   static_assert(!scaled || (ROW == 128 && CH == 1), "one scale block per chunk");
-  static_assert(CG == 1 || (CG == 2 && !scaled && BN % 32 == 0), "CTA pairs: BF16 and TF32 forms");
+  static_assert(CG == 1 || (CG == 2 && E != Elem::E4M3 && BN % 32 == 0), "CTA pairs: BF16, F16 and TF32 forms");
   static_assert(STAGE_TX == CG * STAGE, "pair stage bytes");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert(TMEM_COLS <= 512 && BUF_COLS >= BN, "tensor memory");
@@ -139,6 +144,10 @@ using FormTF32x3_c = Form<Elem::TF32, 2, 3, 128, 3>;
 using FormBF16x6 = Form<Elem::BF16, 3, 6, 128, 2>;
 using FormBF16x6_b = Form<Elem::BF16, 3, 6, 128, 4, 64>;
 using FormBF16x6_c = Form<Elem::BF16, 3, 6, 256, 2, 64>;
+// split-FP16 (fp16x3): the bf16x3 shapes with F16 terms and block scales
+using FormF16x3 = Form<Elem::F16, 2, 3, 256, 2>;
+using FormF16x3_c = Form<Elem::F16, 2, 3, 128, 3>;
+using FormF16x3_p = Form<Elem::F16, 2, 3, 256, 3, 128, 2>;
 using FormFP8 = Form<Elem::E4M3, 1, 1, 128, 6>;
 using FormFP8_w = Form<Elem::E4M3, 1, 1, 256, 4>;  // 128 x 256 tiles: twice the MMA work per scaled chunk
 // CTA-pair configurations (cluster of 2, 256 x 256 tiles)
@@ -179,6 +188,12 @@ struct Term<Elem::BF16> {
   using T = __nv_bfloat16;
   __device__ static T round(float x) { return __float2bfloat16_rn(x); }
   __device__ static float widen(T x) { return __bfloat162float(x); }
+};
+template <>
+struct Term<Elem::F16> {
+  using T = __half;
+  __device__ static T round(float x) { return __float2half_rn(x); }
+  __device__ static float widen(T x) { return __half2float(x); }
 };
 template <>
 struct Term<Elem::TF32> {
@@ -377,19 +392,101 @@ __device__ __forceinline__ void split_convert_mn(const float (&v)[16], typename 
   }
 }
 
+// The row transform of split_convert_kmajor / split_convert_mn applied in
+// place to a thread's values (same arithmetic), for the F16 form, whose
+// block scale is taken after the transform.
+__device__ __forceinline__ void xform_kmajor(float (&v)[16], int R, int64_t r0, int64_t k0, const RowXform& xf, int K) {
+  if(!xf.mean) return;
+  const int tid = threadIdx.x;
+  const int rr = tid >> 4, kc = 4 * (tid & 15);
+#pragma unroll
+  for(int e = 0; e < 4; ++e) {
+    const int64_t r = r0 + rr + 16 * e;
+    if(r >= R) continue;
+    const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
+#pragma unroll
+    for(int i = 0; i < 4; ++i) {
+      float y = v[4 * e + i] - m;
+      if(xf.sd) y = (y / xf.div) / sd;
+      v[4 * e + i] = k0 + kc + i < K ? y : 0.f;
+    }
+  }
+}
+__device__ __forceinline__ void xform_mn(float (&v)[16], int R, int64_t r0, int64_t k0, const RowXform& xf, int K) {
+  if(!xf.mean) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = r0 + 32 * (warp & 1) + lane, kc = k0 + 16 * (warp >> 1);
+  if(r >= R) return;
+  const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
+#pragma unroll
+  for(int i = 0; i < 16; ++i) {
+    float y = v[i] - m;
+    if(xf.sd) y = (y / xf.div) / sd;
+    v[i] = kc + i < K ? y : 0.f;
+  }
+}
+
+// Power-of-two scale s of a 64 x 64 block for F16 terms (all 256 threads):
+// with the block maximum m = f 2^ex (f in [0.5, 1)), s = 2^(15 - ex) puts
+// m s in [2^14, 2^15), so the hi term stays below FP16's largest finite
+// value (65504) and the lo term, about 2^-11 of hi, stays in FP16's normal
+// range for every element within 2^-18 of the block maximum.  Scaling by a
+// power of two is exact; 1/s (also exact) goes to *inv_out for the
+// epilogue.  The maximum is over the finite elements (an infinity or NaN
+// stays one and leaves the block's other elements scaled); an all-zero
+// block gives s = 1.
+__device__ __forceinline__ float block_pow2_scale(const float (&v)[16], float* inv_out) {
+  __shared__ float red[8];
+  float m = 0.f;
+#pragma unroll
+  for(int i = 0; i < 16; ++i) m = fabsf(v[i]) < INFINITY ? fmaxf(m, fabsf(v[i])) : m;  // finite elements
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = red[0];
+#pragma unroll
+  for(int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+  const uint32_t bits = __float_as_uint(m);
+  int e = 0;
+  if(m > 0.f && (bits & 0x7f800000u) != 0x7f800000u) {
+    const int biased = int((bits >> 23) & 0xffu);
+    const int ex = biased == 0 ? -125 : biased - 126;  // m = f 2^ex, f in [0.5, 1) (subnormal m: below that)
+    e = min(max(15 - ex, -120), 120);
+  }
+  if(threadIdx.x == 0) *inv_out = __uint_as_float(uint32_t(127 - e) << 23);
+  return __uint_as_float(uint32_t(127 + e) << 23);
+}
+
 // panel[t][r][k] (r < R, k < Kp) = term t of op(X)[r][k] for k < K, 0 beyond,
 // op(X)[r][k] = X[r*ld + k] (k_major) or X[k*ld + r].  Panels are Kp-strided
-// and `panel_stride` elements apart.  One 64 x 64 block per CTA.
+// and `panel_stride` elements apart.  One 64 x 64 block per CTA.  F16 terms:
+// the block is scaled by a power of two first (block_pow2_scale) and its
+// inverse scale stored at inv_scale[blockIdx.y * gridDim.x + blockIdx.x].
 template <Elem E, int TERMS>
 __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X, int64_t ld, int k_major, int R, int K,
-    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride, RowXform xf) {
+    int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride, RowXform xf, float* __restrict__ inv_scale) {
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
   float v[16];
-  if(k_major) {
+  if(k_major)
     split_load(X, ld, k_major, R, K, r0, k0, v);
+  else
+    split_load_mn(X, ld, R, K, r0, k0, v);
+  if constexpr(E == Elem::F16) {
+    if(k_major)
+      xform_kmajor(v, R, r0, k0, xf, K);
+    else
+      xform_mn(v, R, r0, k0, xf, K);
+    const float s = block_pow2_scale(v, inv_scale + int64_t(blockIdx.y) * gridDim.x + blockIdx.x);
+#pragma unroll
+    for(int i = 0; i < 16; ++i) v[i] *= s;
+    if(k_major)
+      split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0);
+    else
+      split_convert_mn<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0);
+  } else if(k_major) {
     split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
   } else {
-    split_load_mn(X, ld, R, K, r0, k0, v);
     split_convert_mn<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
   }
 }
@@ -589,6 +686,7 @@ struct SingleSched {
   int64_t ldc;
   const float* sl[2] = {nullptr, nullptr};
   const float* sr[2] = {nullptr, nullptr};
+  int kt = 0;  // scaled forms: scale blocks along K (a row of the scale tables)
   // Symmetric updates (syrk, syr2k: the product is symmetric, M == N, BM == BN):
   // only tiles on or below the diagonal are computed; the ones below it also
   // store their transpose.
@@ -631,7 +729,7 @@ struct SingleSched {
       tile_coords(t, (M + BM - 1) / BM, (N + BN - 1) / BN, tm, tn);
     }
     return TileInfo{tm * BM, tn * BN, M, N, Kp, npair, alpha, beta, C, ldc, maps.p, {sl[0], sl[1]}, {sr[0], sr[1]},
-        Kp / 128, lower && tm != tn};
+        kt, lower && tm != tn};
   }
 };
 
@@ -819,11 +917,11 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             const uint64_t db = umma::desc_k<F::ROW>(b_base + prod_b(p) * F::B_TILE + off);
             const uint32_t acc = (it % F::CH != 0 || q > 0) ? 1u : 0u;
             if constexpr(F::CG == 2) {
-              if constexpr(F::elem == Elem::BF16)
+              if constexpr((F::elem == Elem::BF16 || F::elem == Elem::F16))
                 umma::mma_f16_pair(d, da, db, F::IDESC, acc);
               else
                 umma::mma_tf32_pair(d, da, db, F::IDESC, acc);
-            } else if constexpr(F::elem == Elem::BF16) {
+            } else if constexpr((F::elem == Elem::BF16 || F::elem == Elem::F16)) {
               umma::mma_f16(d, da, db, F::IDESC, acc);
             } else if constexpr(F::elem == Elem::TF32) {
               umma::mma_tf32(d, da, db, F::IDESC, acc);
@@ -896,15 +994,35 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
       }
       // E4M3: the block scales of chunk c + 1 are loaded while chunk c is
       // waited for and summed (their global-memory latency off the chunk's path)
-      auto chunk_scale = [&](int cc) -> float {
-        const int pair = cc % ti.npair, kb = cc / ti.npair;
+      // (F16: one scale per 64-column block of the warp's columns, so one per
+      // pair of 32-column groups j)
+      // (rows and columns past the matrix edge, whose sums are not stored,
+      // read the last block's scale: the tables hold the blocks that exist)
+      const int srow = min(ti.m0 + int(rank) * F::BM_CTA + 32 * q, M - 1) / F::SCALE_ROWS;  // scale block of these rows
+      auto chunk_scale = [&](int cc, int j) -> float2 {  // chunk cc = stage iteration it0 + cc (CH = 1)
+        const int pair = (it0 + cc) % ti.npair, kb = (it0 + cc) / ti.npair;
         const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
         const float* sr = pair ? ti.sr[1] : ti.sr[0];
-        return sl[(ti.m0 >> 7) * ti.kt + kb] * sr[(nbase >> 7) * ti.kt + kb];
+        const float l = sl[srow * ti.kt + kb], r = sr[(min(nbase + 32 * j, N - 1) / F::SCALE_ROWS) * ti.kt + kb];
+        if constexpr(F::elem == Elem::F16) {
+          // F16 terms: l = 2^-ea, r = 2^-eb (|ea|, |eb| <= 120), so l r can
+          // leave FP32's range while the chunk times it does not; the
+          // exponent -(ea + eb) is applied in two halves, each a normal float
+          const int e = int((__float_as_uint(l) >> 23) & 0xffu) + int((__float_as_uint(r) >> 23) & 0xffu) - 254;
+          const int e1 = e / 2;
+          return make_float2(__uint_as_float(uint32_t(127 + e1) << 23), __uint_as_float(uint32_t(127 + e - e1) << 23));
+        } else {
+          return make_float2(l * r, 1.f);
+        }
       };
-      float sc_next = 1.f;
+      constexpr int NSC = F::elem == Elem::F16 ? F::HALF / 32 : 1;  // scales per chunk of this warp
+      float2 sc_next[NSC];
+#pragma unroll
+      for(int jj = 0; jj < NSC; ++jj) sc_next[jj] = make_float2(1.f, 1.f);
       if constexpr(F::scaled)
-        if(chunks > 0) sc_next = chunk_scale(0);
+        if(chunks > 0)
+#pragma unroll
+          for(int jj = 0; jj < NSC; ++jj) sc_next[jj] = chunk_scale(0, jj);
       for(int c = 0; c < chunks; ++c, ++chunk) {
         const int b = chunk % F::NBUF;
         // C under this warp's 32 rows x HALF columns (and their mirror) into
@@ -918,10 +1036,15 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
         umma::fence_after_sync();
         const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
-        float sc = 1.f;  // block scale of this chunk (E4M3): left row block x right column block
+        float2 sc[NSC];  // block scale(s) of this chunk: left row block x right column block
+#pragma unroll
+        for(int jj = 0; jj < NSC; ++jj) sc[jj] = make_float2(1.f, 1.f);
         if constexpr(F::scaled) {
-          sc = sc_next;
-          if(c + 1 < chunks) sc_next = chunk_scale(c + 1);
+#pragma unroll
+          for(int jj = 0; jj < NSC; ++jj) {
+            sc[jj] = sc_next[jj];
+            if(c + 1 < chunks) sc_next[jj] = chunk_scale(c + 1, jj);
+          }
         }
 #pragma unroll
         for(int j = 0; j < F::HALF / 32; ++j) {
@@ -930,7 +1053,9 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           umma::tmem_ld_wait();
 #pragma unroll
           for(int i = 0; i < 32; ++i) {
-            const float v = F::scaled ? sc * __uint_as_float(r[i]) : __uint_as_float(r[i]);
+            float v = __uint_as_float(r[i]);
+            if constexpr(F::elem == Elem::E4M3) v *= sc[0].x;
+            if constexpr(F::elem == Elem::F16) v = (v * sc[j].x) * sc[j].y;
             acc[32 * j + i] = (c == 0) ? v : acc[32 * j + i] + v;
           }
         }
@@ -1093,12 +1218,12 @@ struct Panels {
 
 template <class F>
 gbpoly_status launch_split(gbpoly_ctx* ctx, const float* X, int64_t ld, bool k_major, int64_t rows, int64_t K,
-    int64_t Kp, Panels out, RowXform xf = RowXform{}) {
+    int64_t Kp, Panels out, RowXform xf = RowXform{}, float* inv_scale = nullptr) {
   using T = typename Term<F::elem>::T;
   dim3 grid(static_cast<unsigned>(Kp / 64), static_cast<unsigned>((rows + 63) / 64));
   ProfileScope prof(ctx, "split_terms");
   split_kernel<F::elem, F::terms><<<grid, 256, 0, ctx->stream>>>(X, ld, k_major ? 1 : 0, int(rows), int(K), int(Kp),
-      reinterpret_cast<T*>(out.base), int64_t(out.stride / sizeof(T)), xf);
+      reinterpret_cast<T*>(out.base), int64_t(out.stride / sizeof(T)), xf, inv_scale);
   GBPOLY_CUDA_TRY(cudaGetLastError());
   return GBPOLY_OK;
 }
@@ -1107,6 +1232,7 @@ template <class F>
 gbpoly_status make_product_maps(gbpoly_ctx* ctx, ProductMaps& pm, Panels left, int64_t left_rows, Panels right,
     int64_t right_rows, int64_t Kp) {
   const auto dt = F::elem == Elem::BF16   ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                  : F::elem == Elem::F16  ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                   : F::elem == Elem::TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                           : CU_TENSOR_MAP_DATA_TYPE_UINT8;
   const auto sw = F::ROW == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
@@ -1307,13 +1433,21 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
   TailPlan tail;
   gbpoly_status st = plan_tail<F, Sched>(ctx, tiles, (Kp / F::BK) * (a.dual ? 2 : 1), tail);
   if(st != GBPOLY_OK) return st;
-  if((st = ensure_workspace(ctx, a_bytes + b_bytes + tail.bytes)) != GBPOLY_OK) return st;
+  // F16 terms: inverse block scales after the panels, [64-row block][64-K block]
+  const int64_t kt = Kp / 64;
+  const size_t sa_bytes = F::elem == Elem::F16 ? align_up(size_t((a.M + 63) / 64) * size_t(kt) * 4, 256) : 0;
+  const size_t sb_bytes = F::elem == Elem::F16 && !same ? align_up(size_t((a.N + 63) / 64) * size_t(kt) * 4, 256) : 0;
+  if((st = ensure_workspace(ctx, a_bytes + b_bytes + sa_bytes + sb_bytes + tail.bytes)) != GBPOLY_OK) return st;
   char* ws = static_cast<char*>(ctx->ws.ptr);
   Panels pa{ws, a_stride};
   Panels pb = same ? pa : Panels{ws + a_bytes, b_stride};
-  if(a.K > 0) {
-    if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, Kp, pa, a.xf)) != GBPOLY_OK) return st;
-    if(!same && (st = launch_split<F>(ctx, a.B, a.ldb, a.op_b == GBPOLY_OP_T, a.N, a.K, Kp, pb)) != GBPOLY_OK)
+  float* const sa = F::elem == Elem::F16 ? reinterpret_cast<float*>(ws + a_bytes + b_bytes) : nullptr;
+  float* const sb = same ? sa : (F::elem == Elem::F16 ? reinterpret_cast<float*>(ws + a_bytes + b_bytes + sa_bytes) : nullptr);
+  if(a.K > 0 || F::elem == Elem::F16) {  // (F16: the split also writes the scales; with K = 0 they are 1)
+    if((st = launch_split<F>(ctx, a.A, a.lda, a.op_a == GBPOLY_OP_N, a.M, a.K, Kp, pa, a.xf, sa)) != GBPOLY_OK)
+      return st;
+    if(!same && (st = launch_split<F>(ctx, a.B, a.ldb, a.op_b == GBPOLY_OP_T, a.N, a.K, Kp, pb, RowXform{}, sb)) !=
+                    GBPOLY_OK)
       return st;
   } else {
     GBPOLY_CUDA_TRY(cudaMemsetAsync(ws, 0, a_bytes + b_bytes, ctx->stream));
@@ -1331,13 +1465,18 @@ gbpoly_status run_form(gbpoly_ctx* ctx, const GemmF32Args& a, const char* kernel
 
   Sched sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
   sched.lower = lower;
+  if constexpr(F::elem == Elem::F16) {
+    sched.sl[0] = sa, sched.sr[0] = sb;
+    sched.sl[1] = sb, sched.sr[1] = sa;  // syr2k's second pairing, B_i . A_j^T
+    sched.kt = int(kt);
+  }
   if constexpr(F::CEPI) {
     if(lower || !c_tile_ok(a)) return fail(GBPOLY_ERR_UNSUPPORTED, "C-tile epilogue: non-symmetric, 16-byte-aligned C");
     if((st = make_tmap_2d(ctx, &sched.cmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.C, a.M, a.N, a.ldc, 32, 32,
             CU_TENSOR_MAP_SWIZZLE_128B)) != GBPOLY_OK)
       return st;
   }
-  if((st = apply_tail(ctx, tail, ws + a_bytes + b_bytes, sched)) != GBPOLY_OK) return st;
+  if((st = apply_tail(ctx, tail, ws + a_bytes + b_bytes + sa_bytes + sb_bytes, sched)) != GBPOLY_OK) return st;
   return launch_tc_kernel<F>(ctx, sched, tail.units, kernel_name);
 }
 
@@ -1378,6 +1517,7 @@ gbpoly_status run_fp8(gbpoly_ctx* ctx, const GemmF32Args& a) {
   SingleSched<F::BM, F::BN> sched{maps, npair, int(a.M), int(a.N), int(Kp), a.alpha, a.beta, a.C, a.ldc};
   sched.sl[0] = sa;
   sched.sr[0] = sb;
+  sched.kt = int(kb);
   if(a.dual) {  // syr2k: B_i . A_j^T
     sched.npair = 2;
     if((st = make_product_maps<F>(ctx, sched.maps.p[1], pb, a.M, pa, a.N, Kp)) != GBPOLY_OK) return st;
@@ -1410,6 +1550,11 @@ size_t workspace_bytes(gbpoly_precision prec, int64_t M, int64_t N, int64_t K, b
   case GBPOLY_PREC_BF16X3: return bytes_of<FormBF16x3>(M, N, K, same) + tail;
   case GBPOLY_PREC_TF32X3: return bytes_of<FormTF32x3>(M, N, K, same) + tail;
   case GBPOLY_PREC_BF16X6: return bytes_of<FormBF16x6>(M, N, K, same) + tail;
+  case GBPOLY_PREC_FP16X3: {
+    const size_t kt = align_up(size_t(std::max<int64_t>(K, 1)), 64) / 64;
+    return bytes_of<FormF16x3>(M, N, K, same) + tail + align_up(size_t((M + 63) / 64) * kt * 4, 256) +
+           (same ? 0 : align_up(size_t((N + 63) / 64) * kt * 4, 256));
+  }
   case GBPOLY_PREC_FP8: {
     const size_t Kp = align_up(size_t(std::max<int64_t>(K, 1)), 128), kb = Kp / 128;
     return align_up(size_t(M) * Kp, 1024) + (same ? 0 : align_up(size_t(N) * Kp, 1024)) +
@@ -1429,6 +1574,7 @@ int tensor_config_count(gbpoly_precision prec) {
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6: return 6;  // configurations 3, 4, 5: CTA pairs (5: C tile in shared memory)
   case GBPOLY_PREC_FP8: return 2;  // configuration 1: 128 x 256 tiles
+  case GBPOLY_PREC_FP16X3: return 3;  // 0: 128 x 256, 1: 128 x 128, 2: CTA pairs 256 x 256
   default: return 0;
   }
 }
@@ -1461,6 +1607,9 @@ gbpoly_status launch_gemm_tensor_config(gbpoly_ctx* ctx, gbpoly_precision prec, 
   case GBPOLY_PREC_BF16X6 * 8 + 5: return run_form<FormBF16x6_t>(ctx, a, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8<FormFP8>(ctx, a);
   case GBPOLY_PREC_FP8 * 8 + 1: return run_fp8<FormFP8_w>(ctx, a);
+  case GBPOLY_PREC_FP16X3 * 8 + 0: return run_form<FormF16x3>(ctx, a, "fp16x3_gemm");
+  case GBPOLY_PREC_FP16X3 * 8 + 1: return run_form<FormF16x3_c>(ctx, a, "fp16x3_gemm");
+  case GBPOLY_PREC_FP16X3 * 8 + 2: return run_form<FormF16x3_p>(ctx, a, "fp16x3_gemm");
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
 }
@@ -1500,6 +1649,7 @@ bool config_is_square(gbpoly_precision prec, int config) {
   case GBPOLY_PREC_TF32X3: return config == 2 || config == 3 || config == 4;
   case GBPOLY_PREC_BF16X6: return config == 0 || config == 1 || config == 3 || config == 4;
   case GBPOLY_PREC_FP8: return config == 0;
+  case GBPOLY_PREC_FP16X3: return config == 1 || config == 2;
   default: return false;
   }
 }
@@ -1508,6 +1658,7 @@ bool pairs_fill(gbpoly_ctx* ctx, int64_t pair_tiles) { return pair_tiles >= std:
 int square_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t N) {
   if(prec == GBPOLY_PREC_FP8) return 0;
   const int64_t t = (N + 255) / 256;
+  if(prec == GBPOLY_PREC_FP16X3) return pairs_fill(ctx, t * (t + 1) / 2) ? 2 : 1;
   if(pairs_fill(ctx, t * (t + 1) / 2)) return 3;
   return prec == GBPOLY_PREC_BF16X6 ? 1 : 2;
 }
@@ -1523,6 +1674,8 @@ int default_config(gbpoly_ctx* ctx, gbpoly_precision prec, int64_t M, int64_t N,
   // fp8: 128 x 256 tiles (twice the MMA work per scaled chunk: 1.38x at
   // N = 8192) when they give every SM a tile, else 128 x 128
   if(prec == GBPOLY_PREC_FP8) return ((M + 127) / 128) * ((N + 255) / 256) >= ctx->sm_count ? 1 : 0;
+  // fp16x3: CTA pairs when they fill the device, else 128 x 128 tiles
+  if(prec == GBPOLY_PREC_FP16X3) return pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256)) ? 2 : 1;
   if(tensor_config_count(prec) <= 3) return 0;
   if(pairs_fill(ctx, ((M + 255) / 256) * ((N + 255) / 256))) {
     const int64_t k_tile = prec == GBPOLY_PREC_TF32 ? 512 : (prec == GBPOLY_PREC_TF32X3 ? 128 : 256);
@@ -1569,6 +1722,10 @@ gbpoly_status tensor_plan_panel(gbpoly_ctx* ctx, const TensorPlan& plan, const G
   case GBPOLY_PREC_BF16X6 * 8 + 4: return run_form_panel<FormBF16x6_q>(ctx, a, plan.M, first, r0, "bf16x6_gemm");
   case GBPOLY_PREC_FP8 * 8 + 0: return run_fp8<FormFP8>(ctx, a);  // quantises both operands per panel
   case GBPOLY_PREC_FP8 * 8 + 1: return run_fp8<FormFP8_w>(ctx, a);
+  // fp16x3: split both operands (and their block scales) per panel
+  case GBPOLY_PREC_FP16X3 * 8 + 0: return run_form<FormF16x3>(ctx, a, "fp16x3_gemm");
+  case GBPOLY_PREC_FP16X3 * 8 + 1: return run_form<FormF16x3_c>(ctx, a, "fp16x3_gemm");
+  case GBPOLY_PREC_FP16X3 * 8 + 2: return run_form<FormF16x3_p>(ctx, a, "fp16x3_gemm");
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form or tile configuration not available");
   }
 }

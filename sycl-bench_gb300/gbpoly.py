@@ -46,6 +46,7 @@ class Precision(enum.IntEnum):
     FP8 = 3
     TF32X3 = 4
     BF16X6 = 5
+    FP16X3 = 6
 
 
 class Op(enum.IntEnum):

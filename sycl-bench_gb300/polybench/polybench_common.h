@@ -4,7 +4,7 @@
 //    polybench/common/polybenchUtilFuncts.h:27-42 (float narrowing kept).
 //  * Benchmark-specific options, read through args.cli like the reference's
 //    own extra options (include/command_line.h:98-103):
-//      --precision=fp32|bf16x3|tf32|tf32x3|bf16x6|fp8[,...]  form(s) to run (fp32)
+//      --precision=fp32|bf16x3|tf32|tf32x3|bf16x6|fp16x3|fp8[,...]  form(s) to run (fp32)
 //      --init=polybench|uniform|normal          input initialisation (polybench)
 //      --seed=<u64>                             seed of uniform/normal inputs (1)
 //      --alpha=<f> --beta=<f>                   override syrk/syr2k/gemm scalars
@@ -73,6 +73,7 @@ inline const char* precision_name(gbpoly_precision p) {
   case GBPOLY_PREC_FP8: return "fp8";
   case GBPOLY_PREC_TF32X3: return "tf32x3";
   case GBPOLY_PREC_BF16X6: return "bf16x6";
+  case GBPOLY_PREC_FP16X3: return "fp16x3";
   }
   return "?";
 }
@@ -84,6 +85,7 @@ inline gbpoly_precision parse_precision(const std::string& s) {
   if(s == "fp8") return GBPOLY_PREC_FP8;
   if(s == "tf32x3") return GBPOLY_PREC_TF32X3;
   if(s == "bf16x6") return GBPOLY_PREC_BF16X6;
+  if(s == "fp16x3") return GBPOLY_PREC_FP16X3;
   throw std::invalid_argument{"unknown --precision value: " + s};
 }
 
@@ -100,7 +102,8 @@ inline std::vector<gbpoly_precision> precisions(const BenchmarkArgs& args) {
 // Precision forms whose split pass can centre (and scale) the columns of the
 // covariance / correlation data itself (gbpoly_covariance_f32).
 inline bool centres_in_split(gbpoly_precision p) {
-  return p == GBPOLY_PREC_TF32 || p == GBPOLY_PREC_BF16X3 || p == GBPOLY_PREC_TF32X3 || p == GBPOLY_PREC_BF16X6;
+  return p == GBPOLY_PREC_TF32 || p == GBPOLY_PREC_BF16X3 || p == GBPOLY_PREC_TF32X3 || p == GBPOLY_PREC_BF16X6 ||
+         p == GBPOLY_PREC_FP16X3;
 }
 
 inline void require_fp32_only(const BenchmarkArgs& args) {

@@ -9,8 +9,9 @@ from gbpoly import Op, Precision
 
 pytestmark = pytest.mark.gpu
 
-FORMS = [Precision.TF32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
-BOUND = {Precision.TF32: 1e-3, Precision.BF16X3: 2e-5, Precision.TF32X3: 5e-6, Precision.BF16X6: 5e-6}
+FORMS = [Precision.TF32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.FP16X3]
+BOUND = {Precision.TF32: 1e-3, Precision.BF16X3: 2e-5, Precision.TF32X3: 5e-6, Precision.BF16X6: 5e-6,
+         Precision.FP16X3: 5e-6}
 
 
 @pytest.mark.parametrize("prec", FORMS)
@@ -35,7 +36,7 @@ def test_every_configuration_is_correct(ctx, prec, op_b):
     ctx.config_set(prec, M, N, K, 0)
 
 
-@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.BF16X6])
+@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.BF16X6, Precision.FP16X3])
 def test_every_configuration_runs_syr2k(ctx, prec):
     n, k = 264, 200
     rng = np.random.default_rng(8)

@@ -31,7 +31,7 @@ COV_FLOAT_N = np.float32(3214212.01)          # covariance.cpp:18
 CORR_FLOAT_N = 3214212.01                     # correlation.cpp:12 (double)
 CORR_EPS = 0.005
 SIZES = [1, 2, 7, 16, 37, 64, 100, 255, 256, 257, 640, 1024]
-FORMS = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
+FORMS = [Precision.FP32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.FP16X3]
 
 
 def ldp_of(n):

@@ -1,4 +1,4 @@
-"""Parity of the tensor-core forms (tf32, bf16x3, tf32x3, bf16x6) against the
+"""Parity of the tensor-core forms (tf32, bf16x3, tf32x3, bf16x6, fp16x3) against the
 oracle, through the C ABI.
 
 Tolerances: the reference's verify rule (every element within 0.05 percent
@@ -7,6 +7,7 @@ and a normwise Frobenius error against the FP64 oracle on random inputs of
   tf32    1e-3   (operands rounded to 11 significand bits)
   bf16x3  2e-5   (hi+lo BF16 keep ~16 bits: ~2^-17 per operand)
   tf32x3, bf16x6: the FP32 bound 2e-6*sqrt(K) (the terms keep ~24 bits)
+  fp16x3  the same bound (hi+lo FP16 of block-scaled operands keep 22 bits)
 """
 import numpy as np
 import pytest
@@ -17,8 +18,8 @@ from gbpoly import Op, Precision
 pytestmark = pytest.mark.gpu
 
 P = Precision.BF16X3
-FORMS = [Precision.TF32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
-VERIFYING = [Precision.BF16X3, Precision.TF32X3, Precision.BF16X6]
+FORMS = [Precision.TF32, Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.FP16X3]
+VERIFYING = [Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.FP16X3]
 
 
 def frob_bound(prec, K):
@@ -80,7 +81,8 @@ BF16X3_ERR, BF16X3_RATIO = 4.44e-6, 21.3
 def test_error_relative_to_fp32(ctx):
     """Error against the FP64 oracle relative to plain FP32's, normal(0,1) inputs.
 
-    tf32x3 and bf16x6 keep ~24 significand bits per operand and match FP32;
+    tf32x3 and bf16x6 keep ~24 significand bits per operand and match FP32,
+    fp16x3 keeps 22 (2^-23 relative per operand) and matches it too;
     bf16x3 keeps ~16, so its error is set by its operands' representation
     (about 2^-17 relative), not by K: at K = 512, where FP32's accumulation
     error is still small (2.1e-7), it is 4.4e-6, BF16X3_RATIO times FP32's, as
@@ -98,11 +100,12 @@ def test_error_relative_to_fp32(ctx):
     f32 = err[Precision.FP32]
     assert err[Precision.TF32X3] < 1.5 * f32
     assert err[Precision.BF16X6] < 1.5 * f32
+    assert err[Precision.FP16X3] < 1.5 * f32
     assert err[Precision.BF16X3] < 1.5 * BF16X3_RATIO * f32
     assert err[Precision.BF16X3] < 1.5 * BF16X3_ERR
 
 
-@pytest.mark.parametrize("prec", [Precision.TF32X3, Precision.BF16X6])
+@pytest.mark.parametrize("prec", [Precision.TF32X3, Precision.BF16X6, Precision.FP16X3])
 def test_long_k_error_no_worse_than_fp32(ctx, prec):
     """K = 8192 on the polybench gemm inputs (all positive: truncation bias
     would add up): the 24-bit forms stay within FP32's error."""
