@@ -449,6 +449,18 @@ def run_gpu(args, dist: Dist) -> dict | None:
     }
 
 
+# the arithmetic each form computes in (inputs and outputs are FP32 for every form)
+DTYPE_OF_FORM = {
+    "fp32": "f32",
+    "bf16x3": "bf16x3 (f32 in/out, bf16 hi/lo products, f32 accumulate)",
+    "bf16x6": "bf16x6 (f32 in/out, three bf16 terms, 6 products, f32 accumulate)",
+    "fp16x3": "fp16x3 (f32 in/out, fp16 hi/lo of power-of-two-scaled 64x64 blocks, f32 accumulate)",
+    "tf32x3": "tf32x3 (f32 in/out, tf32 hi/lo products, f32 accumulate)",
+    "tf32": "tf32 (f32 in/out, f32 accumulate)",
+    "fp8": "e4m3 (f32 in/out, one scale per 128x128 block, f32 accumulate)",
+}
+
+
 def matched_error(tiers: dict) -> dict | None:
     """The fastest tensor-core form whose normwise and Frobenius errors against
     FP64 are both no larger than plain FP32's, on the polybench and on the
@@ -563,8 +575,8 @@ def run_family(ctx, args) -> dict:
     E, F, G = work
     res = {}
     for prec in forms:
-        # the split forms with a grouped kernel: E and F (independent) as one grouped launch, then G
-        plan = None if prec in (Precision.FP32, Precision.FP16X3) else ctx.grouped_plan(prec, ctx.descs([
+        # the split forms: E and F (independent) as one grouped launch, then G
+        plan = None if prec == Precision.FP32 else ctx.grouped_plan(prec, ctx.descs([
             {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": A, "lda": n, "B": B, "ldb": n, "C": E, "ldc": n},
             {"M": n, "N": n, "K": n, "alpha": 1.0, "beta": 0.0, "A": Cm, "lda": n, "B": D, "ldb": n, "C": F,
              "ldc": n}]))
@@ -581,8 +593,7 @@ def run_family(ctx, args) -> dict:
         r = {"stage1_E": err(E, c64), "stage2_F": err(F, e64), "end_to_end_G": err(G, g64)}
         g = graph_of(stages) if prec != Precision.FP32 else None
         r.update(time_steps((lambda: ctx.graph_launch(g)) if g else stages, 6.0 * n ** 3))
-        r["mode"] = ("grouped E,F + G in one CUDA graph" if plan is not None else "three launches in one CUDA graph") \
-            if g else "three launches"
+        r["mode"] = "grouped E,F + G in one CUDA graph" if g else "three launches"
         if g:
             ctx.graph_destroy(g)
         if plan is not None:
@@ -973,7 +984,8 @@ def run_grouped_workload(ctx, args) -> dict:
                        f"log-uniform [1e-3,1e3]", "flops_per_step": flops}
     descs = ctx.descs(items)
     for prec, mode in ((Precision.FP32, "per-GEMM launches"), (Precision.BF16X3, "grouped plan in a CUDA graph"),
-                       (Precision.BF16X6, "grouped plan in a CUDA graph")):
+                       (Precision.BF16X6, "grouped plan in a CUDA graph"),
+                       (Precision.FP16X3, "grouped plan in a CUDA graph")):
         tuned = None
         if prec != Precision.FP32:  # the grouped autotuner picks the tile configuration for this problem class
             tuned = ctx.autotune_grouped(prec, descs, reps=3)
@@ -1141,7 +1153,7 @@ def main() -> None:
             r["seconds"] * 1e3 for r in samples), dtype="f32",
             cpu_baseline={"value": val, "unit": "TFLOP/s", "cores": best["cores"], "kind": "port",
                           "sample": f"first {best['rows']} of {n} output rows of the gemm.cpp:82-91 kernel body, "
-                                    f"OpenMP over (row, 64-wide column block), -O3 -march=native -ffast-math"},
+                                    f"OpenMP over (row, 64-wide column block), -O3 -ffast-math"},
             e2e={"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
         print(json.dumps(line))
         dist.close()
@@ -1153,10 +1165,10 @@ def main() -> None:
         r = cpu_gemm_sample(n, args.cpu_seconds)
         cpu = {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["cores"], "kind": "port",
                "sample": f"first {r['rows']} of {n} output rows of the gemm.cpp:82-91 kernel body on the host "
-                         f"cores ({r['seconds']:.1f} s), oracle port built -O3 -march=native -ffast-math"}
+                         f"cores ({r['seconds']:.1f} s), oracle port built -O3 -ffast-math"}
     if dist.rank == 0:
         line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"],
-                    dtype="f32" if res["headline"] == "fp32" else "bf16x3 (f32 in/out, bf16 hi/lo products, f32 accumulate)",
+                    dtype=DTYPE_OF_FORM[res["headline"]],
                     e2e=res["e2e"], roofline=res["roofline"], cpu_baseline=cpu, clocks=res["clocks"],
                     err_vs_fp64=res["err_vs_fp64"], matched_error=res["matched_error"],
                     gpu_launches=res["gpu_launches"], tiers=res["tiers"], headline_form=res["headline"],

@@ -88,7 +88,7 @@ def lib() -> ct.CDLL:
 
 
 def fast_lib() -> ct.CDLL:
-    """The reference's release-flag build (-O3 -march=native -ffast-math), for timing only."""
+    """The reference's release-flag build (-O3 -ffast-math; no -march=native), for timing only."""
     global _fast
     if _fast is None:
         _fast = _load(LIB_FAST)

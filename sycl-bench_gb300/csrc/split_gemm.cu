@@ -435,8 +435,9 @@ __device__ __forceinline__ void xform_mn(float (&v)[16], int R, int64_t r0, int6
 // epilogue.  The maximum is over the finite elements (an infinity or NaN
 // stays one and leaves the block's other elements scaled); an all-zero
 // block gives s = 1.
-__device__ __forceinline__ float block_pow2_scale(const float (&v)[16], float* inv_out) {
-  __shared__ float red[8];
+// red: 8 words of shared memory (a loop over blocks alternates two sets, so
+// that a warp ahead by one block never overwrites words still being read).
+__device__ __forceinline__ float block_pow2_scale(const float (&v)[16], float* inv_out, float* red) {
   float m = 0.f;
 #pragma unroll
   for(int i = 0; i < 16; ++i) m = fabsf(v[i]) < INFINITY ? fmaxf(m, fabsf(v[i])) : m;  // finite elements
@@ -477,7 +478,8 @@ __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X,
       xform_kmajor(v, R, r0, k0, xf, K);
     else
       xform_mn(v, R, r0, k0, xf, K);
-    const float s = block_pow2_scale(v, inv_scale + int64_t(blockIdx.y) * gridDim.x + blockIdx.x);
+    __shared__ float red[8];
+    const float s = block_pow2_scale(v, inv_scale + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, red);
 #pragma unroll
     for(int i = 0; i < 16; ++i) v[i] *= s;
     if(k_major)
@@ -499,6 +501,7 @@ struct SplitJob {
   int k_major, R, K, Kp;
   void* out;
   int64_t panel_stride;  // elements
+  float* scale;          // F16 terms: inverse block scales, [row block][Kp / 64]
 };
 
 // Grouped split pass: persistent CTAs walk the blocks in a grid-stride loop
@@ -517,7 +520,8 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
   int4 bl = blocks[b];
   SplitJob j = jobs[bl.x];
   int4 bl_next = b + int(gridDim.x) < nblocks ? blocks[b + gridDim.x] : make_int4(0, 0, 0, 0);
-  while(true) {
+  __shared__ float red[2][8];  // F16: block maxima, alternating sets
+  for(int iter = 0;; ++iter) {
     const int64_t r0 = int64_t(bl.y) * 64, k0 = int64_t(bl.z) * 64;
     float v[16];
     if(j.k_major)
@@ -527,6 +531,11 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
     const int nb = b + int(gridDim.x);
     const SplitJob jn = jobs[bl_next.x];  // in flight with this block's loads
     const int4 bl_after = nb + int(gridDim.x) < nblocks ? blocks[nb + gridDim.x] : make_int4(0, 0, 0, 0);
+    if constexpr(E == Elem::F16) {
+      const float s = block_pow2_scale(v, j.scale + int64_t(bl.y) * (j.Kp / 64) + bl.z, red[iter & 1]);
+#pragma unroll
+      for(int i = 0; i < 16; ++i) v[i] *= s;
+    }
     if(j.k_major)
       split_convert_kmajor<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
     else
@@ -740,6 +749,8 @@ struct GroupProblem {
   float alpha, beta;
   float* C;
   int64_t ldc;
+  const float* sa;  // F16 terms: inverse block scales of A and B, [row block][Kp / 64]
+  const float* sb;
 };
 template <int BM, int BN>
 struct GroupedSched {
@@ -756,8 +767,8 @@ struct GroupedSched {
   __device__ TileInfo tile(int t) const {
     const int4 e = tiles[t];
     const GroupProblem p = probs[e.x];
-    return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x,
-        {nullptr, nullptr}, {nullptr, nullptr}, 0, false};
+    return TileInfo{e.y * BM, e.z * BN, p.M, p.N, p.Kp, 1, p.alpha, p.beta, p.C, p.ldc, maps + e.x, {p.sa, p.sa},
+        {p.sb, p.sb}, p.Kp / 64, false};
   }
 };
 
@@ -992,73 +1003,54 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           ++c_loads;
         }
       }
-      // E4M3: the block scales of chunk c + 1 are loaded while chunk c is
-      // waited for and summed (their global-memory latency off the chunk's path)
-      // (F16: one scale per 64-column block of the warp's columns, so one per
-      // pair of 32-column groups j)
-      // (rows and columns past the matrix edge, whose sums are not stored,
-      // read the last block's scale: the tables hold the blocks that exist)
-      const int srow = min(ti.m0 + int(rank) * F::BM_CTA + 32 * q, M - 1) / F::SCALE_ROWS;  // scale block of these rows
-      auto chunk_scale = [&](int cc, int j) -> float2 {  // chunk cc = stage iteration it0 + cc (CH = 1)
-        const int pair = (it0 + cc) % ti.npair, kb = (it0 + cc) / ti.npair;
-        const float* sl = pair ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
-        const float* sr = pair ? ti.sr[1] : ti.sr[0];
-        const float l = sl[srow * ti.kt + kb], r = sr[(min(nbase + 32 * j, N - 1) / F::SCALE_ROWS) * ti.kt + kb];
-        if constexpr(F::elem == Elem::F16) {
-          // F16 terms: l = 2^-ea, r = 2^-eb (|ea|, |eb| <= 120), so l r can
-          // leave FP32's range while the chunk times it does not; the
-          // exponent -(ea + eb) is applied in two halves, each a normal float
-          const int e = int((__float_as_uint(l) >> 23) & 0xffu) + int((__float_as_uint(r) >> 23) & 0xffu) - 254;
-          const int e1 = e / 2;
-          return make_float2(__uint_as_float(uint32_t(127 + e1) << 23), __uint_as_float(uint32_t(127 + e - e1) << 23));
-        } else {
-          return make_float2(l * r, 1.f);
+      // Scaled forms (E4M3, F16): chunk c (stage iteration it0 + c, CH = 1)
+      // is multiplied by the factor of its left row block and right column
+      // block, for each of the NCB blocks the warp's columns span.  Lane t
+      // computes the factors of chunk 32 g + t for a whole group g of 32
+      // chunks, one group ahead (its loads then have 32 chunks to land), and
+      // every chunk takes its factors from lane c % 32 by shuffle: two scale
+      // loads per lane per 32 chunks, not per thread per chunk.  Rows and
+      // columns past the matrix edge, whose sums are not stored, read the
+      // last block's scales (the tables hold the blocks that exist).
+      constexpr int NCB = F::scaled && F::HALF > F::SCALE_ROWS ? F::HALF / F::SCALE_ROWS : 1;
+      // factors of the current group's and the next group's chunk at this
+      // lane: x alone, or x then y when one factor would leave FP32's range
+      float fx[NCB], fy[NCB], nx[NCB], ny[NCB];
+      auto load_group = [&](int g, float(&x)[NCB], float(&y)[NCB]) {
+        const int cc = 32 * g + lane;
+#pragma unroll
+        for(int cb = 0; cb < NCB; ++cb) x[cb] = 1.f, y[cb] = 1.f;
+        if(cc >= chunks) return;
+        const int it = it0 + cc;
+        const bool second = ti.npair == 2 && (it & 1);  // syr2k: iterations alternate the two pairings
+        const int kb = ti.npair == 2 ? it >> 1 : it;
+        const float* sl = second ? ti.sl[1] : ti.sl[0];  // selects, not indexing: keeps TileInfo in registers
+        const float* sr = second ? ti.sr[1] : ti.sr[0];
+        const int srow = min(crow, M - 1) / F::SCALE_ROWS;
+        const float l = sl[srow * ti.kt + kb];
+#pragma unroll
+        for(int cb = 0; cb < NCB; ++cb) {
+          const float r = sr[(min(nbase + F::SCALE_ROWS * cb, N - 1) / F::SCALE_ROWS) * ti.kt + kb];
+          if constexpr(F::elem == Elem::F16) {
+            // l = 2^-ea, r = 2^-eb with |ea|, |eb| <= 120: the factor
+            // 2^-(ea + eb) is a normal float, or else two halves of it are
+            const int e = int((__float_as_uint(l) >> 23) & 0xffu) + int((__float_as_uint(r) >> 23) & 0xffu) - 254;
+            const int e1 = e >= -126 && e <= 127 ? e : (e >> 1);
+            x[cb] = __uint_as_float(uint32_t(127 + e1) << 23);
+            y[cb] = __uint_as_float(uint32_t(127 + e - e1) << 23);
+          } else {
+            x[cb] = l * r;
+          }
         }
       };
-      constexpr int NSC = F::elem == Elem::F16 ? F::HALF / 32 : 1;  // scales per chunk of this warp
-      float2 sc_next[NSC];
-#pragma unroll
-      for(int jj = 0; jj < NSC; ++jj) sc_next[jj] = make_float2(1.f, 1.f);
-      if constexpr(F::scaled)
-        if(chunks > 0)
-#pragma unroll
-          for(int jj = 0; jj < NSC; ++jj) sc_next[jj] = chunk_scale(0, jj);
-      for(int c = 0; c < chunks; ++c, ++chunk) {
-        const int b = chunk % F::NBUF;
-        // C under this warp's 32 rows x HALF columns (and their mirror) into
-        // L2 a few chunks before the tile's end, ahead of the epilogue's
-        // loads (prefetching the next tile's C a whole epilogue ahead was
-        // slower: 178 -> 190 us at M = N = 8192, K = 64)
-        if(!F::CEPI && c == max(0, chunks - 4) && beta != 0.f && role != 2) prefetch_c_warp<F>(ti, rank, q, h, lane);
-        if(!mbar_wait(&chunk_full[b], (chunk / F::NBUF) & 1, err, kDevErrMmaWait)) {
-          ok = false;
-          break;
-        }
-        umma::fence_after_sync();
-        const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
-        float2 sc[NSC];  // block scale(s) of this chunk: left row block x right column block
-#pragma unroll
-        for(int jj = 0; jj < NSC; ++jj) sc[jj] = make_float2(1.f, 1.f);
-        if constexpr(F::scaled) {
-#pragma unroll
-          for(int jj = 0; jj < NSC; ++jj) {
-            sc[jj] = sc_next[jj];
-            if(c + 1 < chunks) sc_next[jj] = chunk_scale(c + 1, jj);
-          }
-        }
-#pragma unroll
-        for(int j = 0; j < F::HALF / 32; ++j) {
-          uint32_t r[32];
-          umma::tmem_ld_32x32b_x32(base + 32 * j, r);
-          umma::tmem_ld_wait();
-#pragma unroll
-          for(int i = 0; i < 32; ++i) {
-            float v = __uint_as_float(r[i]);
-            if constexpr(F::elem == Elem::E4M3) v *= sc[0].x;
-            if constexpr(F::elem == Elem::F16) v = (v * sc[j].x) * sc[j].y;
-            acc[32 * j + i] = (c == 0) ? v : acc[32 * j + i] + v;
-          }
-        }
+      if constexpr(F::scaled) load_group(0, fx, fy);
+      // chunk buffers of chunk c: C under this warp's 32 rows x HALF columns
+      // (and their mirror) is prefetched into L2 a few chunks before the
+      // tile's end, ahead of the epilogue's loads (prefetching the next
+      // tile's C a whole epilogue ahead was slower: 178 -> 190 us at
+      // M = N = 8192, K = 64); the chunk's buffer is released on the first
+      // CTA's barrier when its columns are in registers
+      auto release = [&](int b) {
         umma::fence_before_sync();
         __syncwarp();
         if(lane == 0) {
@@ -1066,6 +1058,83 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             mbar_arrive_cluster(b ? chunk_empty_pair[1] : chunk_empty_pair[0]);
           else
             mbar_arrive(&chunk_empty[b]);
+        }
+      };
+      if constexpr(F::scaled) {
+        // chunk c: its factors from lane c % 32, then acc = chunk x factor + acc
+        auto consume = [&](int c) -> bool {
+          const int b = chunk % F::NBUF;
+          if(!F::CEPI && c == max(0, chunks - 4) && beta != 0.f && role != 2) prefetch_c_warp<F>(ti, rank, q, h, lane);
+          if(!mbar_wait(&chunk_full[b], (chunk / F::NBUF) & 1, err, kDevErrMmaWait)) return false;
+          umma::fence_after_sync();
+          const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
+          float x[NCB], y[NCB];
+          bool single = true;  // every y is 1 (the same in all lanes: one row block, the same column blocks)
+#pragma unroll
+          for(int cb = 0; cb < NCB; ++cb) {
+            x[cb] = __shfl_sync(0xffffffffu, fx[cb], c & 31);
+            y[cb] = 1.f;
+            if constexpr(F::elem == Elem::F16) {
+              y[cb] = __shfl_sync(0xffffffffu, fy[cb], c & 31);
+              single = single && y[cb] == 1.f;
+            }
+          }
+#pragma unroll
+          for(int j = 0; j < F::HALF / 32; ++j) {
+            uint32_t r[32];
+            umma::tmem_ld_32x32b_x32(base + 32 * j, r);
+            umma::tmem_ld_wait();
+            const int cb = min(32 * j / F::SCALE_ROWS, NCB - 1);
+            if(single) {
+#pragma unroll
+              for(int i = 0; i < 32; ++i)
+                acc[32 * j + i] = fmaf(__uint_as_float(r[i]), x[cb], c == 0 ? 0.f : acc[32 * j + i]);
+            } else {
+#pragma unroll
+              for(int i = 0; i < 32; ++i)
+                acc[32 * j + i] = fmaf(__uint_as_float(r[i]) * x[cb], y[cb], c == 0 ? 0.f : acc[32 * j + i]);
+            }
+          }
+          release(b);
+          return true;
+        };
+        // groups of 32 chunks, the next group's factors loaded as each
+        // group starts (outside the chunk loop, so that they are not
+        // predicated into every chunk)
+        for(int c0 = 0; c0 < chunks && ok; c0 += 32) {
+          if(c0 > 0) {
+#pragma unroll
+            for(int cb = 0; cb < NCB; ++cb) fx[cb] = nx[cb], fy[cb] = ny[cb];
+          }
+          load_group(c0 / 32 + 1, nx, ny);
+          for(int c = c0; c < min(chunks, c0 + 32); ++c, ++chunk)
+            if(!consume(c)) {
+              ok = false;
+              break;
+            }
+        }
+      } else {
+        for(int c = 0; c < chunks; ++c, ++chunk) {
+          const int b = chunk % F::NBUF;
+          if(!F::CEPI && c == max(0, chunks - 4) && beta != 0.f && role != 2) prefetch_c_warp<F>(ti, rank, q, h, lane);
+          if(!mbar_wait(&chunk_full[b], (chunk / F::NBUF) & 1, err, kDevErrMmaWait)) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(b) * F::BUF_COLS + uint32_t(h * F::HALF);
+#pragma unroll
+          for(int j = 0; j < F::HALF / 32; ++j) {
+            uint32_t r[32];
+            umma::tmem_ld_32x32b_x32(base + 32 * j, r);
+            umma::tmem_ld_wait();
+#pragma unroll
+            for(int i = 0; i < 32; ++i) {
+              const float v = __uint_as_float(r[i]);
+              acc[32 * j + i] = (c == 0) ? v : acc[32 * j + i] + v;
+            }
+          }
+          release(b);
         }
       }
       if(!ok) continue;
@@ -1762,7 +1831,7 @@ struct gbpoly_grouped {
   int4* split_table = nullptr;  // split block -> (job, row block, k block, 0)
   int ntiles = 0, njobs = 0, split_blocks = 0;
   int64_t flops = 0;
-  int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3) 128 x 256
+  int config = 0;  // tile configuration: 0 128 x 128, 1 CTA pairs 256 x 256, 2 (bf16x3, fp16x3) 128 x 256
 };
 
 namespace gbpoly {
@@ -1782,6 +1851,16 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
     off += F::terms * align_up(size_t(d.M) * kp[i] * F::esz, 1024);
     b_off[i] = off;
     off += F::terms * align_up(size_t(d.N) * kp[i] * F::esz, 1024);
+  }
+  // F16 terms: each operand's inverse block scales after the panels
+  std::vector<size_t> sa_off(P), sb_off(P);
+  for(int i = 0; i < P; ++i) {
+    const auto& d = g->descs[i];
+    if(F::elem != Elem::F16) continue;
+    sa_off[i] = off = align_up(off, 256);
+    off += size_t((d.M + 63) / 64) * size_t(kp[i] / 64) * 4;
+    sb_off[i] = off = align_up(off, 256);
+    off += size_t((d.N + 63) / 64) * size_t(kp[i] / 64) * 4;
   }
   const size_t probs_off = align_up(off, 256), maps_off = align_up(probs_off + P * sizeof(GroupProblem), 128);
   std::vector<int4> tiles;
@@ -1819,17 +1898,19 @@ gbpoly_status plan_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   gbpoly_status st;
   for(int i = 0; i < P; ++i) {
     const auto& d = g->descs[i];
-    probs[i] = GroupProblem{int(d.M), int(d.N), int(kp[i]), 0, d.alpha, d.beta, d.C, d.ldc};
+    float* const scale_a = F::elem == Elem::F16 ? reinterpret_cast<float*>(base + sa_off[i]) : nullptr;
+    float* const scale_b = F::elem == Elem::F16 ? reinterpret_cast<float*>(base + sb_off[i]) : nullptr;
+    probs[i] = GroupProblem{int(d.M), int(d.N), int(kp[i]), 0, d.alpha, d.beta, d.C, d.ldc, scale_a, scale_b};
     const size_t sa = align_up(size_t(d.M) * kp[i] * F::esz, 1024), sb = align_up(size_t(d.N) * kp[i] * F::esz, 1024);
     Panels pa{base + a_off[i], sa}, pb{base + b_off[i], sb};
     if(d.M > 0 && d.N > 0) {
       if((st = make_product_maps<F>(ctx, maps[i], pa, d.M, pb, d.N, kp[i])) != GBPOLY_OK) return st;
       const int kb = int(kp[i] / 64);
       jobs.push_back(SplitJob{d.A, d.lda, d.op_a == GBPOLY_OP_N ? 1 : 0, int(d.M), int(d.K), int(kp[i]), pa.base,
-          int64_t(sa / F::esz)});
+          int64_t(sa / F::esz), scale_a});
       add_blocks(d.M, kb);
       jobs.push_back(SplitJob{d.B, d.ldb, d.op_b == GBPOLY_OP_T ? 1 : 0, int(d.N), int(d.K), int(kp[i]), pb.base,
-          int64_t(sb / F::esz)});
+          int64_t(sb / F::esz), scale_b});
       add_blocks(d.N, kb);
     }
     g->flops += 2 * d.M * d.N * d.K;
@@ -1870,8 +1951,8 @@ gbpoly_status run_grouped(gbpoly_ctx* ctx, gbpoly_grouped* g, const char* name) 
 
 // Tile configurations of grouped plans: 0 = 1-CTA 128 x 128 tiles (least
 // padding of small problems), 1 = CTA pairs on 256 x 256 tiles (a few large
-// products, as matmulchain's two independent stages), and for bf16x3 2 =
-// 1-CTA 128 x 256 tiles.  Untuned, a group uses 1 when every problem is
+// products, as matmulchain's two independent stages), and for bf16x3 and
+// fp16x3 2 = 1-CTA 128 x 256 tiles.  Untuned, a group uses 1 when every problem is
 // large enough that 256 x 256 tiles pad it about as little as 128 x 128 ones
 // and the group fills at least two rounds of pairs, else 0; the autotuner
 // (gbpoly_autotune_grouped) times them per problem class.
@@ -1884,6 +1965,9 @@ using GroupBF16x3_p = FormBF16x3_p;
 using GroupTF32x3_p = FormTF32x3_p;
 using GroupBF16x6_p = FormBF16x6_p;
 using GroupTF32_p = FormTF32_p;
+using GroupF16x3 = FormF16x3_c;
+using GroupF16x3_p = FormF16x3_p;
+using GroupF16x3_w = FormF16x3;
 
 bool grouped_pairs(gbpoly_ctx* ctx, const std::vector<gbpoly_gemm_desc>& descs) {
   double work128 = 0, work256 = 0;
@@ -1902,7 +1986,8 @@ bool grouped_pairs(gbpoly_ctx* ctx, const std::vector<gbpoly_gemm_desc>& descs) 
 
 int grouped_config_count(gbpoly_precision prec) {
   switch(prec) {
-  case GBPOLY_PREC_BF16X3: return 3;
+  case GBPOLY_PREC_BF16X3:
+  case GBPOLY_PREC_FP16X3: return 3;
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6:
   case GBPOLY_PREC_TF32: return 2;
@@ -1948,7 +2033,7 @@ gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec
     }
   }
   if(prec != GBPOLY_PREC_FP32 && prec != GBPOLY_PREC_BF16X3 && prec != GBPOLY_PREC_TF32X3 &&
-      prec != GBPOLY_PREC_BF16X6 && prec != GBPOLY_PREC_TF32)
+      prec != GBPOLY_PREC_BF16X6 && prec != GBPOLY_PREC_TF32 && prec != GBPOLY_PREC_FP16X3)
     return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   auto* g = new gbpoly_grouped();
   g->prec = prec;
@@ -1974,6 +2059,7 @@ gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec
   case GBPOLY_PREC_TF32X3:
   case GBPOLY_PREC_BF16X6:
   case GBPOLY_PREC_TF32:
+  case GBPOLY_PREC_FP16X3:
     g->config = config >= 0 ? config : default_grouped_config(ctx, prec, descs, count);
     if(g->config >= grouped_config_count(prec)) {
       st = fail(GBPOLY_ERR_INVALID, "no such grouped tile configuration");
@@ -1988,6 +2074,9 @@ gbpoly_status gbpoly::grouped_plan_config(gbpoly_ctx* ctx, gbpoly_precision prec
     case GBPOLY_PREC_BF16X6 * 4: st = plan_grouped<GroupBF16x6>(ctx, g); break;
     case GBPOLY_PREC_BF16X6 * 4 + 1: st = plan_grouped<GroupBF16x6_p>(ctx, g); break;
     case GBPOLY_PREC_TF32 * 4: st = plan_grouped<GroupTF32>(ctx, g); break;
+    case GBPOLY_PREC_FP16X3 * 4: st = plan_grouped<GroupF16x3>(ctx, g); break;
+    case GBPOLY_PREC_FP16X3 * 4 + 1: st = plan_grouped<GroupF16x3_p>(ctx, g); break;
+    case GBPOLY_PREC_FP16X3 * 4 + 2: st = plan_grouped<GroupF16x3_w>(ctx, g); break;
     default: st = plan_grouped<GroupTF32_p>(ctx, g); break;
     }
     break;
@@ -2032,6 +2121,10 @@ gbpoly_status gbpoly_grouped_run(gbpoly_ctx* ctx, gbpoly_grouped* g) {
   case GBPOLY_PREC_TF32:
     return g->config == 1 ? run_grouped<GroupTF32_p>(ctx, g, "grouped_tf32_gemm")
                           : run_grouped<GroupTF32>(ctx, g, "grouped_tf32_gemm");
+  case GBPOLY_PREC_FP16X3:
+    return g->config == 1   ? run_grouped<GroupF16x3_p>(ctx, g, "grouped_fp16x3_gemm")
+           : g->config == 2 ? run_grouped<GroupF16x3_w>(ctx, g, "grouped_fp16x3_gemm")
+                            : run_grouped<GroupF16x3>(ctx, g, "grouped_fp16x3_gemm");
   default: return fail(GBPOLY_ERR_UNSUPPORTED, "precision form not available for grouped calls");
   }
 }

@@ -15,7 +15,7 @@ from gbpoly import Op, Precision
 pytestmark = pytest.mark.gpu
 
 BOUND = {Precision.FP32: 2e-5, Precision.TF32: 2e-3, Precision.BF16X3: 3e-5, Precision.TF32X3: 5e-6,
-         Precision.BF16X6: 5e-6}
+         Precision.BF16X6: 5e-6, Precision.FP16X3: 5e-6}
 
 
 def make_problems(rng, count, lo, hi):
@@ -145,6 +145,50 @@ def test_grouped_large_problems_run_on_cta_pairs(ctx, prec):
         np.testing.assert_array_equal(got.view(np.uint32), single.view(np.uint32))
         for b in (dA, dB, dS):
             ctx.free(b)
+    ctx.grouped_destroy(plan)
+    for b in bufs:
+        for x in b:
+            ctx.free(x)
+
+
+# fp16x3 grouped tile configuration -> the single-call configuration with the same tiles
+FP16X3_SINGLE_OF_GROUPED = {0: 1, 1: 2, 2: 0}
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_grouped_fp16x3_is_bitwise_the_single_calls(ctx, cfg):
+    # the grouped split pass writes the same FP16 terms and block scales as a
+    # single call's, and the tiles sum the same chunks in the same order
+    rng = np.random.default_rng(41 + cfg)
+    prec = Precision.FP16X3
+    probs = []
+    for i, (M, N, K) in enumerate([(700, 520, 333), (256, 384, 64), (130, 1000, 450), (1024, 512, 700)]):
+        op_a = Op.T if i == 2 else Op.N
+        op_b = Op.T if i == 1 else Op.N
+        A = (rng.uniform(-1, 1, (K, M) if op_a == Op.T else (M, K)) * 10.0 ** (i - 2)).astype(np.float32)
+        B = rng.uniform(-1, 1, (N, K) if op_b == Op.T else (K, N)).astype(np.float32)
+        C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+        probs.append((op_a, op_b, M, N, K, A, B, C))
+    descs, bufs = group_descs(ctx, probs)
+    ctx.grouped_config_set(prec, descs, cfg)
+    plan = ctx.grouped_plan(prec, descs)
+    assert ctx.grouped_config_of(plan) == cfg
+    ctx.grouped_run(plan)
+    ctx.synchronize()
+    ctx.tail_split(False)
+    try:
+        for (op_a, op_b, M, N, K, A, B, C), (_, _, dC) in zip(probs, bufs):
+            got = ctx.download(dC, (M, N))
+            dA, dB, dS = ctx.upload(A), ctx.upload(B), ctx.upload(C)
+            ctx.config_set(prec, M, N, K, FP16X3_SINGLE_OF_GROUPED[cfg])
+            ctx.gemm(prec, M, N, K, 1.0, dA, A.shape[1], dB, B.shape[1], 0.5, dS, N, op_a=op_a, op_b=op_b)
+            ctx.synchronize()
+            ctx.config_set(prec, M, N, K, 0)
+            np.testing.assert_array_equal(got.view(np.uint32), ctx.download(dS, (M, N)).view(np.uint32))
+            for b in (dA, dB, dS):
+                ctx.free(b)
+    finally:
+        ctx.tail_split(True)
     ctx.grouped_destroy(plan)
     for b in bufs:
         for x in b:
