@@ -28,11 +28,11 @@ def run(bench, *args):
 
 @pytest.mark.parametrize("bench", list(BENCHES))
 def test_all_forms_verify_on_gpu(bench):
-    out = run(bench, "--size=320", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6")
+    out = run(bench, "--size=320", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6,fp16x3")
     names = re.findall(r"Results for (\S+?)\*", out)
     base = BENCHES[bench]
-    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6", base + "_fp64"]
-    assert out.count("Verification: PASS") == 5, out
+    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6", base + "_fp16x3", base + "_fp64"]
+    assert out.count("Verification: PASS") == 6, out
     assert "kernel-time-mean: N/A" not in out
     assert "NVIDIA" in out or "GB" in out  # device-name is the CUDA device
 
@@ -74,22 +74,23 @@ def test_graph_mode_verifies(bench):
 def test_3mm_grouped_mode_verifies(flags):
     # E and F as one grouped launch (with or without the graph); the double
     # variant keeps its three launches
-    out = run("3mm", "--size=300", "--num-runs=2", *flags, "--precision=fp32,bf16x3")
+    out = run("3mm", "--size=300", "--num-runs=2", *flags, "--precision=fp32,bf16x3,fp16x3")
     base = BENCHES["3mm"]
     names = re.findall(r"Results for (\S+?)\*", out)
     sfx = "_grouped" + ("_graph" if "--graph" in flags else "")
-    assert names == [base + sfx, base + "_bf16x3" + sfx, base + "_fp64" + ("_graph" if "--graph" in flags else "")]
-    assert out.count("Verification: PASS") == 3, out
+    assert names == [base + sfx, base + "_bf16x3" + sfx, base + "_fp16x3" + sfx,
+                     base + "_fp64" + ("_graph" if "--graph" in flags else "")]
+    assert out.count("Verification: PASS") == 4, out
 
 
 @pytest.mark.parametrize("size", [257, 1024])
 @pytest.mark.parametrize("bench", list(FLOAT_ONLY))
 def test_float_only_benchmarks_verify_on_gpu(bench, size):
-    out = run(bench, f"--size={size}", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6")
+    out = run(bench, f"--size={size}", "--num-runs=2", "--precision=fp32,bf16x3,tf32x3,bf16x6,fp16x3")
     names = re.findall(r"Results for (\S+?)\*", out)
     base = FLOAT_ONLY[bench]
-    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6"]
-    assert out.count("Verification: PASS") == 4, out
+    assert names == [base, base + "_bf16x3", base + "_tf32x3", base + "_bf16x6", base + "_fp16x3"]
+    assert out.count("Verification: PASS") == 5, out
     if bench == "matmulchain":  # run() without events, as the reference
         assert "kernel-time-mean: N/A" in out
     else:
@@ -101,8 +102,9 @@ def test_matmulchain_graph_grouped_and_seeded(tmp_path):
     names = re.findall(r"Results for (\S+?)\*", out)
     assert names == ["MatmulChain_grouped_graph", "MatmulChain_bf16x3_grouped_graph"]
     assert out.count("Verification: PASS") == 2, out
-    out = run("matmulchain", "--size=384", "--num-runs=1", "--grouped", "--precision=tf32x3")
-    assert "Results for MatmulChain_tf32x3_grouped" in out and "Verification: PASS" in out
+    out = run("matmulchain", "--size=384", "--num-runs=1", "--grouped", "--precision=tf32x3,fp16x3")
+    assert "Results for MatmulChain_tf32x3_grouped" in out and "Results for MatmulChain_fp16x3_grouped" in out
+    assert out.count("Verification: PASS") == 2, out
     rep = tmp_path / "m.jsonl"
     out = run("matmulchain", "--size=512", "--num-runs=1", "--init=uniform", "--precision=fp32,bf16x3",
               f"--error-report={rep}")
@@ -115,11 +117,11 @@ def test_matmulchain_graph_grouped_and_seeded(tmp_path):
 @pytest.mark.parametrize("bench", ["covariance", "correlation"])
 def test_statistics_benchmarks_error_report_on_gpu(bench, tmp_path):
     rep = tmp_path / "s.jsonl"
-    out = run(bench, "--size=1000", "--num-runs=1", "--precision=fp32,bf16x3,tf32x3", f"--error-report={rep}")
-    assert out.count("Verification: PASS") == 3, out
+    out = run(bench, "--size=1000", "--num-runs=1", "--precision=fp32,bf16x3,tf32x3,fp16x3", f"--error-report={rep}")
+    assert out.count("Verification: PASS") == 4, out
     import json
     rows = [json.loads(x) for x in rep.read_text().splitlines()]
-    assert len(rows) == 3 and all(r["frob_rel"] < 1e-5 for r in rows), rows
+    assert len(rows) == 4 and all(r["frob_rel"] < 1e-5 for r in rows), rows
 
 
 @pytest.mark.parametrize("size", [1024, 4099])
