@@ -33,6 +33,7 @@ import numpy as np  # noqa: E402
 ALPHA, BETA = 32412.0, 2123.0
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+L2_BYTES = 126 << 20  # GB300's L2 (both dies)
 # DRAM bytes (read + write) per launch of the dominant kernel, keyed by
 # (kernel, N, tile configuration): ncu's dram__bytes_read.sum +
 # dram__bytes_write.sum from one capture of the same kernel, configuration
@@ -767,11 +768,33 @@ def run_neighbours(ctx, args) -> dict:
     peaks, _ = load_peaks()
     hbm = peaks.get("hbm_gbs")
 
-    def time_steps(step, steps=None, warmup=None):
+    flush_buf = None
+
+    def time_steps(step, steps=None, warmup=None, flush=False):
+        """Mean ms per step.  flush: an operand smaller than L2 (atax at the
+        suite's 4096: 64 MB) would stay in L2 across back-to-back calls, so
+        each timed step gets its own event pair and a 512 MB write between
+        steps, outside the events, evicts it."""
+        nonlocal flush_buf
         steps, warmup = steps or args.steps, warmup or args.warmup
         for _ in range(warmup):
             step()
         ctx.synchronize()
+        if flush:
+            if flush_buf is None:
+                flush_buf = ctx.alloc(512 << 20)
+            evs = [(ctx.event(), ctx.event()) for _ in range(steps)]
+            for a, b in evs:
+                ctx.memset(flush_buf, 1, 512 << 20)
+                a.record()
+                step()
+                b.record()
+            ctx.synchronize()
+            ms = sum(a.elapsed_ms(b) for a, b in evs) / steps
+            for a, b in evs:
+                a.destroy()
+                b.destroy()
+            return ms
         e0, e1 = ctx.event(), ctx.event()
         e0.record()
         for _ in range(steps):
@@ -922,11 +945,14 @@ def run_neighbours(ctx, args) -> dict:
         ctx.synchronize()
         errs = [float(np.linalg.norm(ctx.download(o, (m,)).astype(np.float64) - r) / np.linalg.norm(r))
                 for o, r in zip(outs, refs)]
-        ms = time_steps(step, steps=max(args.steps, 20))
         matrix_bytes = (2 if name == "gesummv" else 1) * m * m * 4
+        l2_resident = matrix_bytes < 2 * L2_BYTES
+        ms = time_steps(step, steps=max(args.steps, 20), flush=l2_resident)
         gbs = matrix_bytes / (ms * 1e-3) / 1e9
         mv[name] = {"size": m, "us_per_call": ms * 1e3, "matrix_gbs": gbs,
                     "frac_of_hbm": gbs / hbm if hbm else None, "matrix_passes": passes,
+                    "l2": "flushed between steps (512 MB write outside the step's events)" if l2_resident else
+                          "matrix larger than L2",
                     "frob_rel_vs_fp64": max(errs)}
         for b in (dA, d1, d2, y1, y2) + ((dB,) if dB is not None else ()):
             ctx.free(b)
