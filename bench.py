@@ -370,8 +370,10 @@ def run_gpu(args, dist: Dist) -> dict | None:
     dist.barrier()
     e0, e1 = ctx.event(), ctx.event()
     e0.record()
+    t_enq = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
+    enqueue_ms = (time.perf_counter() - t_enq) * 1e3 / args.steps  # host time to issue one call's copies and launches
     e1.record()
     ctx.synchronize()
     e2e_ms = dist.max(e0.elapsed_ms(e1) / args.steps)
@@ -396,11 +398,35 @@ def run_gpu(args, dist: Dist) -> dict | None:
         return c0.elapsed_ms(c1) / (3 * reps)
     h2d_gbs = nbytes / (copy_ms(True) * 1e-3) / 1e9
     d2h_gbs = nbytes / (copy_ms(False) * 1e-3) / 1e9
+
+    # both directions at once, as inside the e2e call (read-back of one panel
+    # beside the next panels' input copies): a second context's stream copies
+    # device -> host while this one copies host -> device
+    ctx2 = gbpoly.Context(dist.local_rank)
+    dtmp2 = ctx2.alloc(nbytes)
+
+    def both_s(reps: int = 3) -> float:
+        ctx.synchronize()
+        ctx2.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for hin, hout in ((hA, hB), (hB, hC), (hC, hA)):
+                gbpoly._check(ctx.lib.gbpoly_memcpy_h2d(ctx.handle, gbpoly._ptr(dtmp), ct.c_void_p(hin), nbytes))
+                gbpoly._check(ctx2.lib.gbpoly_memcpy_d2h(ctx2.handle, ct.c_void_p(hout), gbpoly._ptr(dtmp2), nbytes))
+        ctx.synchronize()
+        ctx2.synchronize()
+        return (time.perf_counter() - t0) / (3 * reps)
+    both_s(1)
+    both_gbs = 2 * nbytes / both_s() / 1e9
+    ctx2.free(dtmp2)
+    ctx2.close()
     ctx.free(dtmp)
     h2d_only_ms = 3 * nbytes / (h2d_gbs * 1e9) * 1e3
-    link = {"h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs,
+    link = {"h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs, "h2d_and_d2h_at_once_total_gbs": both_gbs,
+            "host_enqueue_ms_per_call": enqueue_ms,
             "h2d_bytes_alone_ms": h2d_only_ms, "e2e_frac_of_h2d_bound": h2d_only_ms / e2e_ms,
-            "measured": "plain pinned cudaMemcpyAsync of N^2 x 4 B, same buffers, same run, one direction at a time"}
+            "measured": "plain pinned cudaMemcpyAsync of N^2 x 4 B, same buffers, same run: one direction at a time, "
+                        "then both at once on two streams (host clock)"}
     for p in (hA, hB, hC):
         ctx.lib.gbpoly_host_free(ctx.handle, ct.c_void_p(p))
 

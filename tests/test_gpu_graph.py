@@ -10,7 +10,7 @@ from gbpoly import Precision
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec", [Precision.FP32, Precision.BF16X3, Precision.BF16X6])
+@pytest.mark.parametrize("prec", [Precision.FP32, Precision.BF16X3, Precision.BF16X6, Precision.FP16X3])
 def test_2mm_graph_replay_matches_eager(ctx, prec):
     n = 384
     A, B, C, D = oracle.init_mm2(n)
@@ -52,3 +52,31 @@ def test_workspace_growth_during_capture_is_refused():
             fresh.graph_destroy(g)
         assert e.value.status == gbpoly.Status.STATE
         fresh.synchronize()
+
+
+@pytest.mark.parametrize("prec", [Precision.BF16X3, Precision.TF32X3, Precision.BF16X6, Precision.FP16X3, Precision.TF32])
+@pytest.mark.parametrize("mnk", [(1000, 700, 333), (2304, 2048, 512), (130, 4100, 70)])
+def test_workspace_query_covers_every_configuration(prec, mnk):
+    """A fresh context reserved with gbpoly_workspace_query's bytes captures the
+    call in every tile configuration without growing its workspace (fp16x3's
+    block-scale tables and the K-split tail's partial sums included)."""
+    M, N, K = mnk
+    rng = np.random.default_rng(M + N + K)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    ref = oracle.gemm_f64(A, B, None, 1.0, 0.0)
+    with gbpoly.Context(0) as fresh:
+        dA, dB, dC = fresh.upload(A), fresh.upload(B), fresh.alloc(M * N * 4)
+        fresh.workspace_reserve(fresh.workspace_query(prec, M, N, K))
+        for cfg in range(fresh.config_count(prec)):
+            fresh.config_set(prec, M, N, K, cfg)
+            fresh.graph_begin()
+            try:
+                fresh.gemm(prec, M, N, K, 1.0, dA, K, dB, N, 0.0, dC, N)
+            finally:
+                g = fresh.graph_end()
+            fresh.graph_launch(g)
+            fresh.synchronize()
+            fresh.graph_destroy(g)
+            bound = 1e-3 if prec == Precision.TF32 else 2e-5
+            assert oracle.error_norms(fresh.download(dC, (M, N)), ref)[1] < bound, cfg
