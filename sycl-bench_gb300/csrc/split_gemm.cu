@@ -1044,6 +1044,7 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
         }
       };
       if constexpr(F::scaled) load_group(0, fx, fy);
+      bool group_single = true;  // F16: every chunk of the current group has y = 1
       // chunk buffers of chunk c: C under this warp's 32 rows x HALF columns
       // (and their mirror) is prefetched into L2 a few chunks before the
       // tile's end, ahead of the epilogue's loads (prefetching the next
@@ -1075,8 +1076,10 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
             x[cb] = __shfl_sync(0xffffffffu, fx[cb], c & 31);
             y[cb] = 1.f;
             if constexpr(F::elem == Elem::F16) {
-              y[cb] = __shfl_sync(0xffffffffu, fy[cb], c & 31);
-              single = single && y[cb] == 1.f;
+              if(!group_single) {
+                y[cb] = __shfl_sync(0xffffffffu, fy[cb], c & 31);
+                single = single && y[cb] == 1.f;
+              }
             }
           }
 #pragma unroll
@@ -1105,6 +1108,14 @@ __global__ void __launch_bounds__(F::THREADS, 1) split_gemm_kernel(const __grid_
           if(c0 > 0) {
 #pragma unroll
             for(int cb = 0; cb < NCB; ++cb) fx[cb] = nx[cb], fy[cb] = ny[cb];
+          }
+          if constexpr(F::elem == Elem::F16) {
+            // the whole group needs one factor per block (the usual case):
+            // its chunks skip the second factor's shuffles
+            bool one = true;
+#pragma unroll
+            for(int cb = 0; cb < NCB; ++cb) one = one && fy[cb] == 1.f;
+            group_single = __all_sync(0xffffffffu, one);
           }
           load_group(c0 / 32 + 1, nx, ny);
           for(int c = c0; c < min(chunks, c0 + 32); ++c, ++chunk)
