@@ -1301,6 +1301,7 @@ gbpoly_status launch_split(gbpoly_ctx* ctx, const float* X, int64_t ld, bool k_m
     int64_t Kp, Panels out, RowXform xf = RowXform{}, float* inv_scale = nullptr) {
   using T = typename Term<F::elem>::T;
   dim3 grid(static_cast<unsigned>(Kp / 64), static_cast<unsigned>((rows + 63) / 64));
+  if(grid.y > 65535u) return fail(GBPOLY_ERR_UNSUPPORTED, "operand too large for the split pass (over 65535 row blocks)");
   ProfileScope prof(ctx, "split_terms");
   split_kernel<F::elem, F::terms><<<grid, 256, 0, ctx->stream>>>(X, ld, k_major ? 1 : 0, int(rows), int(K), int(Kp),
       reinterpret_cast<T*>(out.base), int64_t(out.stride / sizeof(T)), xf, inv_scale);
