@@ -345,7 +345,7 @@ gbpoly_status gbpoly_set_diagonal_f32(gbpoly_ctx* ctx, int64_t n, float value, f
  * covariance / correlation contraction of CovarianceReduce + CovarianceCovar
  * (polybench/covariance.cpp:98-126) and CorrelationReduce + CorrelationCorr
  * (polybench/correlation.cpp:144-178) in one call, without a centred copy of
- * X for the split forms (tf32, bf16x3, tf32x3, bf16x6: the split pass centres
+ * X for the split forms (tf32, bf16x3, tf32x3, bf16x6, fp16x3: the split pass centres
  * each element before splitting it, with the same arithmetic, so the result
  * is bitwise that of centring into a copy and contracting it).  fp32 and fp8
  * centre into a context scratch copy and contract it.  The lower triangle of

@@ -193,8 +193,8 @@ size_t fp32_split_k_bytes(int sm_count, int64_t M, int64_t N, int64_t K);
 // The K split count gbpoly_gemm_f32 uses for an FP32 contraction of this
 // shape on operands the TMA kernel can read (1: no split).
 int fp32_split_k_count(int sm_count, int64_t M, int64_t N, int64_t K);
-// Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6.  The split
-// term panels live in the context workspace.
+// Tensor-core forms (split_gemm.cu): tf32, bf16x3, tf32x3, bf16x6, fp16x3,
+// fp8.  The split term panels live in the context workspace.
 gbpoly_status launch_gemm_tensor(gbpoly_ctx* ctx, gbpoly_precision prec, const GemmF32Args& a);
 // Tile configurations of a tensor-core form (0 for none); launch with an
 // explicit configuration; the configuration the context uses for a shape.

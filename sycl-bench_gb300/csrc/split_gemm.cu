@@ -9,11 +9,14 @@
 //   bf16x3    BF16  2      a0.b0 + a0.b1 + a1.b0                 ~16
 //   tf32x3    TF32  2      a0.b0 + a0.b1 + a1.b0                 ~22-24
 //   bf16x6    BF16  3      a0.b0 + a0.b1 + a1.b0 + a0.b2 + a1.b1 + a2.b0   ~24
+//   fp16x3    FP16  2      a0.b0 + a0.b1 + a1.b0 of x 2^e, one power-of-two
+//                          2^e per 64x64 operand block (FP32's range)        22
 //   fp8       E4M3  1      a0.b0, each operand with one scale per 128x128 block   4
 // Two kernels per call:
 //   * split_kernel (memory bound): writes the K-major term panels of an
-//     operand into the context workspace (transposing through shared memory
-//     when the operand is MN-major), K padded with zeros to the k-block;
+//     operand into the context workspace (an MN-major operand transposed by
+//     the register assignment), K padded with zeros to the k-block; for FP16
+//     terms also each block's inverse scale;
 //   * split_gemm_kernel: persistent (one CTA per SM walks 128 x BN tiles of
 //     C), warp specialised, 384 threads:
 //       warp 0      TMA producer: the term tiles of A (128 rows) and B (BN rows),
@@ -26,7 +29,8 @@
 //                   and commits stages and chunks;
 //       warps 4-11  epilogue (setmaxnreg 208): each warp owns 32 rows (its
 //                   TMEM lane quarter) x BN/2 columns and sums the chunks in
-//                   FP32 registers with round-to-nearest adds, then writes
+//                   FP32 registers with round-to-nearest adds (scaled forms:
+//                   times the chunk's left x right block factor), then writes
 //                   C = alpha*acc + beta*C (through a per-warp staging tile,
 //                   or, in the C-tile configurations, through TMA-loaded and
 //                   TMA-stored boxes of C in shared memory).
@@ -676,8 +680,8 @@ struct TileInfo {
   float* C;
   int64_t ldc;
   const ProductMaps* maps;  // [npair]
-  // E4M3 only: per pairing, scales of the left and right operand blocks,
-  // [row block][k block] with kt k blocks per row block
+  // Scaled forms (E4M3, F16): per pairing, scales of the left and right
+  // operand blocks, [row block][k block] with kt k blocks per row block
   const float* sl[2];
   const float* sr[2];
   int kt;
