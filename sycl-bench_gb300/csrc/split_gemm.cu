@@ -369,31 +369,24 @@ __device__ __forceinline__ void split_convert_kmajor(const float (&v)[16], typen
 template <Elem E, int TERMS>
 __device__ __forceinline__ void split_convert_mn(const float (&v)[16], typename Term<E>::T* __restrict__ out,
     int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0, RowXform xf = RowXform{}, int K = 0) {
-  using T = typename Term<E>::T;
+  // the block through a 64 x 65 shared tile (lane = row when loaded, rows of
+  // 4 consecutive k when written): the panel stores then go out exactly as
+  // split_convert_kmajor's, 128-byte row segments per 16 threads
+  __shared__ float tile[64][65];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r = r0 + 32 * (warp & 1) + lane, kc = k0 + 16 * (warp >> 1);
-  if(r >= R) return;
-  float x[16];
+  const int rl = 32 * (warp & 1) + lane, kl = 16 * (warp >> 1);
+  __syncthreads();  // the tile's previous block (grouped split) has been read
 #pragma unroll
-  for(int i = 0; i < 16; ++i) x[i] = v[i];
-  if(xf.mean) {  // the row's transform, on the elements inside K (the K padding stays zero)
-    const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
+  for(int i = 0; i < 16; ++i) tile[rl][kl + i] = v[i];
+  __syncthreads();
+  const int tid = threadIdx.x;
+  const int rr = tid >> 4, kc = 4 * (tid & 15);
+  float w[16];
 #pragma unroll
-    for(int i = 0; i < 16; ++i) {
-      float y = x[i] - m;
-      if(xf.sd) y = (y / xf.div) / sd;
-      x[i] = kc + i < K ? y : 0.f;
-    }
-  }
-  __align__(16) T t[TERMS][16];
-  SplitTerms<E, TERMS>::run(x, t);
-  constexpr int kVec = 16 * sizeof(T) / 16;  // uint4 per 16 elements
+  for(int e = 0; e < 4; ++e)
 #pragma unroll
-  for(int j = 0; j < TERMS; ++j) {
-    uint4* dst = reinterpret_cast<uint4*>(out + j * panel_stride + r * Kp + kc);
-#pragma unroll
-    for(int w = 0; w < kVec; ++w) dst[w] = reinterpret_cast<const uint4*>(t[j])[w];
-  }
+    for(int i = 0; i < 4; ++i) w[4 * e + i] = tile[rr + 16 * e][kc + i];
+  split_convert_kmajor<E, TERMS>(w, out, panel_stride, R, Kp, r0, k0, xf, K);
 }
 
 // The row transform of split_convert_kmajor / split_convert_mn applied in
