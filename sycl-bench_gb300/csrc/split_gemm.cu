@@ -208,23 +208,22 @@ struct Term<Elem::TF32> {
 
 // ------------------------------------------------------------- split pass --
 // One 64 x 64 block of op(X) at (r0, k0) per CTA of 256 threads (or per
-// iteration of a persistent CTA), without a shared-memory tile: every thread
-// converts 16 values it loaded itself, coalesced in both layouts.
+// iteration of a persistent CTA); every thread loads 16 values with 16-byte
+// loads along the rows of X and converts 16 values:
 //   K-major op(X) (op(X)[r][k] = X[r ld + k], rows contiguous in k):
 //     split_load gives thread t elements [4 (t % 16), +4) of the block's rows
-//     t / 16 + 16 e (e < 4), with 16-byte loads; split_convert_kmajor writes
-//     their terms (8 bytes of BF16 or 16 of TF32 per row and term).
-//   MN-major op(X) (op(X)[r][k] = X[k ld + r]): warp w holds block rows
-//     r = 32 (w % 2) + lane and k in [16 (w / 2), +16); each of its 16 loads
-//     is one 128-byte segment of a row of X across the warp, and the 16
-//     values a lane holds are 16 consecutive k of output row r: the
-//     transposition is the register assignment itself.  split_convert_mn
-//     writes the row's terms (32 bytes of BF16 or 64 of TF32 per term).
+//     t / 16 + 16 e (e < 4); split_convert_kmajor writes their terms (8 bytes
+//     of BF16 or FP16, 16 of TF32 per row and term: 128-byte row segments
+//     per 16 threads).
+//   MN-major op(X) (op(X)[r][k] = X[k ld + r]): split_load reads the block's
+//     k rows of X the same way (thread t: r = 4 (t % 16) + j, k = t / 16 +
+//     16 e), and mn_to_kmajor turns them through a 64 x 65 shared tile into
+//     the K-major assignment, so the rest is the K-major path.
 // Values outside R x K are zero, so the K padding of the panels is written
 // with zeros.  Both convert the same way: terms by SplitTerms, an optional
 // per-row transform first (RowXform).
 //
-// Rows of a K-major operand that do not start on a 16-byte boundary (a
+// Rows of X that do not start on a 16-byte boundary (a
 // leading dimension that is not a multiple of 4, or an offset base) are read
 // with the aligned 16-byte loads that cover them: a row segment starting a
 // floats (a < 4) past a boundary is covered by 17 chunks; lane q of a half
@@ -282,15 +281,6 @@ __device__ __forceinline__ void split_load(const float* __restrict__ X, int64_t 
 #pragma unroll
     for(int j = 0; j < 4; ++j) v[4 * e + j] = (row_ok && 4 * q + j < in_lim) ? y[j] : 0.f;
   }
-}
-
-__device__ __forceinline__ void split_load_mn(const float* __restrict__ X, int64_t ld, int R, int K, int64_t r0,
-    int64_t k0, float (&v)[16]) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r = r0 + 32 * (warp & 1) + lane, k = k0 + 16 * (warp >> 1);
-  const float* p = X + k * ld + r;
-#pragma unroll
-  for(int i = 0; i < 16; ++i) v[i] = (r < R && k + i < K) ? p[int64_t(i) * ld] : 0.f;
 }
 
 // Terms of NV consecutive values: t[j] = round(x - t[0] - ... - t[j-1]).
@@ -366,32 +356,31 @@ __device__ __forceinline__ void split_convert_kmajor(const float (&v)[16], typen
   }
 }
 
-template <Elem E, int TERMS>
-__device__ __forceinline__ void split_convert_mn(const float (&v)[16], typename Term<E>::T* __restrict__ out,
-    int64_t panel_stride, int R, int Kp, int64_t r0, int64_t k0, RowXform xf = RowXform{}, int K = 0) {
-  // the block through a 64 x 65 shared tile (lane = row when loaded, rows of
-  // 4 consecutive k when written): the panel stores then go out exactly as
-  // split_convert_kmajor's, 128-byte row segments per 16 threads
+// An MN-major block as split_load gives it (k_major = 0: thread t holds the
+// elements r = 4 (t % 16) + j, k = t / 16 + 16 e, from 16-byte loads along
+// the rows of X) turned through a 64 x 65 shared tile into the K-major
+// assignment (rows t / 16 + 16 e, k in [4 (t % 16), +4)), so the transform,
+// the block scale and the panel stores are the K-major path's: 128-byte row
+// segments per 16 threads.  All 256 threads; the first barrier lets a
+// persistent CTA reuse the tile for its next block.
+__device__ __forceinline__ void mn_to_kmajor(const float (&v)[16], float (&w)[16]) {
   __shared__ float tile[64][65];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rl = 32 * (warp & 1) + lane, kl = 16 * (warp >> 1);
-  __syncthreads();  // the tile's previous block (grouped split) has been read
-#pragma unroll
-  for(int i = 0; i < 16; ++i) tile[rl][kl + i] = v[i];
+  const int tid = threadIdx.x, q = tid & 15, o = tid >> 4;
   __syncthreads();
-  const int tid = threadIdx.x;
-  const int rr = tid >> 4, kc = 4 * (tid & 15);
-  float w[16];
 #pragma unroll
   for(int e = 0; e < 4; ++e)
 #pragma unroll
-    for(int i = 0; i < 4; ++i) w[4 * e + i] = tile[rr + 16 * e][kc + i];
-  split_convert_kmajor<E, TERMS>(w, out, panel_stride, R, Kp, r0, k0, xf, K);
+    for(int j = 0; j < 4; ++j) tile[4 * q + j][o + 16 * e] = v[4 * e + j];
+  __syncthreads();
+#pragma unroll
+  for(int e = 0; e < 4; ++e)
+#pragma unroll
+    for(int i = 0; i < 4; ++i) w[4 * e + i] = tile[o + 16 * e][4 * q + i];
 }
 
-// The row transform of split_convert_kmajor / split_convert_mn applied in
-// place to a thread's values (same arithmetic), for the F16 form, whose
-// block scale is taken after the transform.
+// The row transform of split_convert_kmajor applied in place to a thread's
+// values (same arithmetic), for the F16 form, whose block scale is taken
+// after the transform.
 __device__ __forceinline__ void xform_kmajor(float (&v)[16], int R, int64_t r0, int64_t k0, const RowXform& xf, int K) {
   if(!xf.mean) return;
   const int tid = threadIdx.x;
@@ -407,19 +396,6 @@ __device__ __forceinline__ void xform_kmajor(float (&v)[16], int R, int64_t r0, 
       if(xf.sd) y = (y / xf.div) / sd;
       v[4 * e + i] = k0 + kc + i < K ? y : 0.f;
     }
-  }
-}
-__device__ __forceinline__ void xform_mn(float (&v)[16], int R, int64_t r0, int64_t k0, const RowXform& xf, int K) {
-  if(!xf.mean) return;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r = r0 + 32 * (warp & 1) + lane, kc = k0 + 16 * (warp >> 1);
-  if(r >= R) return;
-  const float m = xf.mean[r], sd = xf.sd ? xf.sd[r] : 1.f;
-#pragma unroll
-  for(int i = 0; i < 16; ++i) {
-    float y = v[i] - m;
-    if(xf.sd) y = (y / xf.div) / sd;
-    v[i] = kc + i < K ? y : 0.f;
   }
 }
 
@@ -466,27 +442,22 @@ __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ X,
     int Kp, typename Term<E>::T* __restrict__ out, int64_t panel_stride, RowXform xf, float* __restrict__ inv_scale) {
   const int64_t r0 = int64_t(blockIdx.y) * 64, k0 = int64_t(blockIdx.x) * 64;
   float v[16];
-  if(k_major)
-    split_load(X, ld, k_major, R, K, r0, k0, v);
-  else
-    split_load_mn(X, ld, R, K, r0, k0, v);
+  if(k_major) {
+    split_load(X, ld, 1, R, K, r0, k0, v);
+  } else {
+    float t[16];
+    split_load(X, ld, 0, R, K, r0, k0, t);
+    mn_to_kmajor(t, v);
+  }
   if constexpr(E == Elem::F16) {
-    if(k_major)
-      xform_kmajor(v, R, r0, k0, xf, K);
-    else
-      xform_mn(v, R, r0, k0, xf, K);
+    xform_kmajor(v, R, r0, k0, xf, K);
     __shared__ float red[8];
     const float s = block_pow2_scale(v, inv_scale + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, red);
 #pragma unroll
     for(int i = 0; i < 16; ++i) v[i] *= s;
-    if(k_major)
-      split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0);
-    else
-      split_convert_mn<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0);
-  } else if(k_major) {
-    split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
+    split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0);
   } else {
-    split_convert_mn<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
+    split_convert_kmajor<E, TERMS>(v, out, panel_stride, R, Kp, r0, k0, xf, K);
   }
 }
 
@@ -521,22 +492,22 @@ __global__ void __launch_bounds__(256, 4) grouped_split_kernel(const SplitJob* _
   for(int iter = 0;; ++iter) {
     const int64_t r0 = int64_t(bl.y) * 64, k0 = int64_t(bl.z) * 64;
     float v[16];
-    if(j.k_major)
-      split_load(j.X, j.ld, 1, j.R, j.K, r0, k0, v);
-    else
-      split_load_mn(j.X, j.ld, j.R, j.K, r0, k0, v);
+    split_load(j.X, j.ld, j.k_major, j.R, j.K, r0, k0, v);
     const int nb = b + int(gridDim.x);
     const SplitJob jn = jobs[bl_next.x];  // in flight with this block's loads
     const int4 bl_after = nb + int(gridDim.x) < nblocks ? blocks[nb + gridDim.x] : make_int4(0, 0, 0, 0);
+    if(!j.k_major) {
+      float t[16];
+#pragma unroll
+      for(int i = 0; i < 16; ++i) t[i] = v[i];
+      mn_to_kmajor(t, v);
+    }
     if constexpr(E == Elem::F16) {
       const float s = block_pow2_scale(v, j.scale + int64_t(bl.y) * (j.Kp / 64) + bl.z, red[iter & 1]);
 #pragma unroll
       for(int i = 0; i < 16; ++i) v[i] *= s;
     }
-    if(j.k_major)
-      split_convert_kmajor<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
-    else
-      split_convert_mn<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
+    split_convert_kmajor<E, TERMS>(v, static_cast<T*>(j.out), j.panel_stride, j.R, j.Kp, r0, k0);
     if(nb >= nblocks) break;
     b = nb;
     bl = bl_next;
