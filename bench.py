@@ -265,6 +265,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
     sampler = clock_sampler(dist.local_rank)
     sampler.start()
     timed_window = (0.0, 0.0)
+    windows = {}  # each form's timed region, for its clock record
     tuned = {}
     for prec in forms:
         if prec == Precision.FP32:
@@ -334,6 +335,7 @@ def run_gpu(args, dist: Dist) -> dict | None:
         timed_err = ctx.error_norms(dC, n, dR, n, n, n)
         if prec == headline:
             timed_window = (t0, t1)
+        windows[prec.name.lower()] = (t0, t1)
         top = max(kernels.items(), key=lambda kv: kv[1][1])
         tiers[prec.name.lower()] = {
             "ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12 * dist.world,
@@ -348,6 +350,9 @@ def run_gpu(args, dist: Dist) -> dict | None:
         }
     sampler.stop()
     clocks = sampler.summary(*timed_window)
+    for name, w in windows.items():  # every form's SM clock and power in its own timed region
+        c = sampler.summary(*w)
+        tiers[name]["clocks"] = {k: c.get(k) for k in ("sm_mhz", "sm_mhz_min", "power_w_max", "reasons", "samples")}
 
     # ---- end to end through the C ABI: pinned host buffers, copies inside the timed region
     import ctypes as ct
